@@ -1,0 +1,272 @@
+"""ctypes declarations of the sort C ABI (include/cccl/c/*.h) and the library loader.
+
+The struct layouts mirror c/parallel/include/cccl/c/types.h, radix_sort.h and
+segmented_sort.h of the reference, so these classes bind either library.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libccclsort.so"
+
+# cccl_type_enum (types.h:31-47)
+INT8, INT16, INT32, INT64, UINT8, UINT16, UINT32, UINT64 = range(8)
+FLOAT16, FLOAT32, FLOAT64, STORAGE, BOOLEAN = 8, 9, 10, 11, 12
+POINTER, ITERATOR = 0, 1  # cccl_iterator_kind_t
+ASCENDING, DESCENDING = 0, 1  # cccl_sort_order_t
+PAYLOAD_LTOIR, PAYLOAD_CUBIN = 0, 1
+
+CUDA_SUCCESS = 0
+CUDA_ERROR_INVALID_VALUE = 1
+CUDA_ERROR_NOT_INITIALIZED = 3
+CUDA_ERROR_NOT_SUPPORTED = 801
+CUDA_ERROR_UNKNOWN = 999
+
+
+class TypeInfo(C.Structure):
+    _fields_ = [("size", C.c_size_t), ("alignment", C.c_size_t), ("type", C.c_int)]
+
+
+class Op(C.Structure):
+    _fields_ = [
+        ("type", C.c_int),
+        ("name", C.c_char_p),
+        ("code", C.c_char_p),
+        ("code_size", C.c_size_t),
+        ("code_type", C.c_int),
+        ("size", C.c_size_t),
+        ("alignment", C.c_size_t),
+        ("state", C.c_void_p),
+        ("extra_ltoirs", C.c_void_p),
+        ("extra_ltoir_sizes", C.c_void_p),
+        ("num_extra_ltoirs", C.c_size_t),
+        ("extra_code_types", C.c_void_p),
+    ]
+
+
+class BuildConfig(C.Structure):
+    _fields_ = [
+        ("extra_compile_flags", C.c_void_p),
+        ("num_extra_compile_flags", C.c_size_t),
+        ("extra_include_dirs", C.c_void_p),
+        ("num_extra_include_dirs", C.c_size_t),
+    ]
+
+
+HOST_ADVANCE = C.CFUNCTYPE(None, C.c_void_p, C.c_uint64)
+
+
+class Iterator(C.Structure):
+    _fields_ = [
+        ("size", C.c_size_t),
+        ("alignment", C.c_size_t),
+        ("type", C.c_int),
+        ("advance", Op),
+        ("dereference", Op),
+        ("value_type", TypeInfo),
+        ("state", C.c_void_p),
+        ("host_advance", C.c_void_p),
+    ]
+
+
+_RADIX_KERNELS = [
+    "single_tile",
+    "upsweep",
+    "alt_upsweep",
+    "scan_bins",
+    "downsweep",
+    "alt_downsweep",
+    "histogram",
+    "exclusive_sum",
+    "init_bins_and_counters",
+    "init_lookback",
+    "onesweep",
+]
+
+
+class RadixSortBuildResult(C.Structure):
+    _fields_ = (
+        [
+            ("cc", C.c_int),
+            ("payload", C.c_void_p),
+            ("payload_size", C.c_size_t),
+            ("payload_kind", C.c_int),
+            ("library", C.c_void_p),
+            ("key_type", TypeInfo),
+            ("value_type", TypeInfo),
+        ]
+        + [(k + "_kernel", C.c_void_p) for k in _RADIX_KERNELS]
+        + [("order", C.c_int), ("runtime_policy", C.c_void_p), ("runtime_policy_size", C.c_size_t)]
+        + [(k + "_kernel_lowered_name", C.c_char_p) for k in _RADIX_KERNELS]
+    )
+
+
+_SEG_KERNELS = [
+    "segmented_sort_fallback",
+    "segmented_sort_kernel_small",
+    "segmented_sort_kernel_large",
+    "three_way_partition_init",
+    "three_way_partition",
+]
+
+
+class SegmentedSortBuildResult(C.Structure):
+    _fields_ = [
+        ("cc", C.c_int),
+        ("payload", C.c_void_p),
+        ("payload_size", C.c_size_t),
+        ("payload_kind", C.c_int),
+        ("library", C.c_void_p),
+        ("key_type", TypeInfo),
+        ("offset_type", TypeInfo),
+        ("large_segments_selector_op", Op),
+        ("small_segments_selector_op", Op),
+        ("segmented_sort_fallback_kernel", C.c_void_p),
+        ("segmented_sort_kernel_small", C.c_void_p),
+        ("segmented_sort_kernel_large", C.c_void_p),
+        ("three_way_partition_init_kernel", C.c_void_p),
+        ("three_way_partition_kernel", C.c_void_p),
+        ("runtime_policy", C.c_void_p),
+        ("runtime_policy_size", C.c_size_t),
+        ("partition_runtime_policy", C.c_void_p),
+        ("partition_runtime_policy_size", C.c_size_t),
+        ("order", C.c_int),
+        ("segmented_sort_fallback_kernel_lowered_name", C.c_char_p),
+        ("segmented_sort_kernel_small_lowered_name", C.c_char_p),
+        ("segmented_sort_kernel_large_lowered_name", C.c_char_p),
+        ("three_way_partition_init_kernel_lowered_name", C.c_char_p),
+        ("three_way_partition_kernel_lowered_name", C.c_char_p),
+    ]
+
+
+# Every symbol the headers under include/cccl/c declare.
+EXPORTED_SYMBOLS = [
+    "cccl_serialization_buffer_free",
+    "cccl_device_radix_sort_build",
+    "cccl_device_radix_sort_build_ex",
+    "cccl_device_radix_sort_compile",
+    "cccl_device_radix_sort_load",
+    "cccl_device_radix_sort",
+    "cccl_device_radix_sort_link_ltoir",
+    "cccl_device_radix_sort_serialize",
+    "cccl_device_radix_sort_deserialize",
+    "cccl_device_radix_sort_cleanup",
+    "cccl_device_segmented_sort_build",
+    "cccl_device_segmented_sort_build_ex",
+    "cccl_device_segmented_sort_compile",
+    "cccl_device_segmented_sort_load",
+    "cccl_device_segmented_sort",
+    "cccl_device_segmented_sort_link_ltoir",
+    "cccl_device_segmented_sort_serialize",
+    "cccl_device_segmented_sort_deserialize",
+    "cccl_device_segmented_sort_cleanup",
+]
+
+_lib = None
+
+
+def _declare(lib):
+    P = C.POINTER
+    R = P(RadixSortBuildResult)
+    S = P(SegmentedSortBuildResult)
+    paths = [C.c_char_p] * 4
+    lib.cccl_device_radix_sort_build.argtypes = [R, C.c_int, Iterator, Iterator, Op, C.c_char_p, C.c_int, C.c_int] + paths
+    lib.cccl_device_radix_sort_build_ex.argtypes = lib.cccl_device_radix_sort_build.argtypes + [P(BuildConfig)]
+    lib.cccl_device_radix_sort_compile.argtypes = lib.cccl_device_radix_sort_build_ex.argtypes
+    lib.cccl_device_radix_sort_load.argtypes = [R]
+    lib.cccl_device_radix_sort.argtypes = [
+        RadixSortBuildResult,
+        C.c_void_p,
+        P(C.c_size_t),
+        Iterator,
+        Iterator,
+        Iterator,
+        Iterator,
+        Op,
+        C.c_uint64,
+        C.c_int,
+        C.c_int,
+        C.c_bool,
+        P(C.c_int),
+        C.c_void_p,
+    ]
+    lib.cccl_device_radix_sort_link_ltoir.argtypes = [R, C.c_void_p, C.c_void_p, C.c_size_t]
+    lib.cccl_device_radix_sort_serialize.argtypes = [R, P(C.c_void_p), P(C.c_size_t)]
+    lib.cccl_device_radix_sort_deserialize.argtypes = [R, C.c_void_p, C.c_size_t]
+    lib.cccl_device_radix_sort_cleanup.argtypes = [R]
+
+    lib.cccl_device_segmented_sort_build.argtypes = [S, C.c_int, Iterator, Iterator, Iterator, Iterator, C.c_int, C.c_int] + paths
+    lib.cccl_device_segmented_sort_build_ex.argtypes = lib.cccl_device_segmented_sort_build.argtypes + [P(BuildConfig)]
+    lib.cccl_device_segmented_sort_compile.argtypes = lib.cccl_device_segmented_sort_build_ex.argtypes
+    lib.cccl_device_segmented_sort_load.argtypes = [S]
+    lib.cccl_device_segmented_sort.argtypes = [
+        SegmentedSortBuildResult,
+        C.c_void_p,
+        P(C.c_size_t),
+        Iterator,
+        Iterator,
+        Iterator,
+        Iterator,
+        C.c_uint64,
+        C.c_uint64,
+        Iterator,
+        Iterator,
+        C.c_bool,
+        P(C.c_int),
+        C.c_void_p,
+    ]
+    lib.cccl_device_segmented_sort_link_ltoir.argtypes = [S, C.c_void_p, C.c_void_p, C.c_size_t]
+    lib.cccl_device_segmented_sort_serialize.argtypes = [S, P(C.c_void_p), P(C.c_size_t)]
+    lib.cccl_device_segmented_sort_deserialize.argtypes = [S, C.c_void_p, C.c_size_t]
+    lib.cccl_device_segmented_sort_cleanup.argtypes = [S]
+    lib.cccl_serialization_buffer_free.argtypes = [C.c_void_p]
+    lib.cccl_serialization_buffer_free.restype = None
+    for name in EXPORTED_SYMBOLS:
+        if name != "cccl_serialization_buffer_free":
+            getattr(lib, name).restype = C.c_int
+
+
+CUDA_STUB = Path("/usr/local/cuda/lib64/stubs/libcuda.so")
+
+
+def load_library(allow_driver_stub: bool = False):
+    """Loads the in-tree sort library. Raises when it has not been built: there is no
+    fallback implementation.
+
+    ``allow_driver_stub`` lets a machine without an NVIDIA driver load the library for
+    host-only calls (compile/serialize/argument checks) by pre-loading the toolkit's
+    libcuda stub; any GPU call then fails with CUDA_ERROR_STUB_LIBRARY."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it first (python -m cccl_gb300.build or __graft_entry__.build())"
+            )
+        try:
+            lib = C.CDLL(str(LIB_PATH))
+        except OSError as e:
+            if not (allow_driver_stub and "libcuda" in str(e) and CUDA_STUB.exists()):
+                raise
+            C.CDLL(str(CUDA_STUB), mode=C.RTLD_GLOBAL)
+            lib = C.CDLL(str(LIB_PATH))
+        _declare(lib)
+        _lib = lib
+    return _lib
+
+
+def pointer_iterator(ptr: int, type_enum: int, size: int, alignment: int | None = None) -> Iterator:
+    """A CCCL_POINTER iterator over device memory at ``ptr`` (0 = absent)."""
+    it = Iterator()
+    it.size = 8
+    it.alignment = 8
+    it.type = POINTER
+    it.value_type = TypeInfo(size, alignment or size, type_enum)
+    it.state = ptr or None
+    return it
+
+
+def no_op() -> Op:
+    return Op()

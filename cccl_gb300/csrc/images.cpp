@@ -1,0 +1,38 @@
+// Accessors for the sm_103a cubins linked into the library. The bytes are placed by
+// the build step (cccl_gb300/build.py writes an .incbin stub next to this file's object).
+#include "abi_common.h"
+
+extern "C" {
+extern const unsigned char gb300_img_radix_k1[], gb300_img_radix_k1_end[];
+extern const unsigned char gb300_img_radix_k2[], gb300_img_radix_k2_end[];
+extern const unsigned char gb300_img_radix_k4[], gb300_img_radix_k4_end[];
+extern const unsigned char gb300_img_radix_k8[], gb300_img_radix_k8_end[];
+extern const unsigned char gb300_img_segmented[], gb300_img_segmented_end[];
+}
+
+namespace gb300
+{
+
+image_ref radix_image(int key_bytes)
+{
+  switch (key_bytes)
+  {
+    case 1:
+      return {gb300_img_radix_k1, size_t(gb300_img_radix_k1_end - gb300_img_radix_k1)};
+    case 2:
+      return {gb300_img_radix_k2, size_t(gb300_img_radix_k2_end - gb300_img_radix_k2)};
+    case 4:
+      return {gb300_img_radix_k4, size_t(gb300_img_radix_k4_end - gb300_img_radix_k4)};
+    case 8:
+      return {gb300_img_radix_k8, size_t(gb300_img_radix_k8_end - gb300_img_radix_k8)};
+    default:
+      throw cuda_error(CUDA_ERROR_NOT_SUPPORTED, "no kernels for this key width");
+  }
+}
+
+image_ref segmented_image()
+{
+  return {gb300_img_segmented, size_t(gb300_img_segmented_end - gb300_img_segmented)};
+}
+
+} // namespace gb300

@@ -1,0 +1,5 @@
+// Plain-path kernels for 1-byte keys (integer key kinds).
+#include "radix_instances.cuh"
+
+GB300_ALL_VALUES(1, false, i)
+

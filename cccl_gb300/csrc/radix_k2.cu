@@ -1,0 +1,5 @@
+// Plain-path kernels for 2-byte keys (integer and floating-point key kinds).
+#include "radix_instances.cuh"
+
+GB300_ALL_VALUES(2, false, i)
+GB300_ALL_VALUES(2, true, f)

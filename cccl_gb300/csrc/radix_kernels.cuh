@@ -1,0 +1,597 @@
+// Plain-path radix sort kernels for sm_103a: control-block init, all-pass digit
+// histogram (with the exclusive scan fused into its last CTA), the onesweep digit pass
+// and the single-CTA sort for small inputs.
+//
+// Algorithm (reference roles, file:line in the reference tree):
+//  * histogram of every pass in one read of the keys
+//      cub/cub/agent/agent_radix_sort_histogram.cuh:96-285, kernel_radix_sort.cuh:447-473;
+//    exclusive sum of each pass's bins  kernel_radix_sort.cuh:563-606;
+//  * one stable 8-bit counting-sort pass per digit with decoupled look-back across tiles
+//      cub/cub/agent/agent_radix_sort_onesweep.cuh:152-739, kernel_radix_sort.cuh:498-558;
+//    stable in-tile ranking with per-warp digit counters and warp match
+//      cub/cub/block/block_radix_rank.cuh:913-1213;
+//  * small inputs sorted by one CTA  kernel_radix_sort.cuh:330-434.
+//
+// Differences in how the work is laid out on GB300 (same results):
+//  * tiles are staged in up to ~100 KB of dynamic shared memory (CUB caps static shared
+//    memory at 48 KB), giving longer same-digit runs in the scatter;
+//  * keys stay in the encoded (bit-ordered, order-applied) form between passes, so the
+//    encode runs on the first pass's load and the decode on the last pass's store only;
+//  * every look-back wait is bounded (wait_status) and reports a status bit instead of
+//    spinning forever;
+//  * the look-back buffer of the next pass is cleared by the current pass (row per tile),
+//    so no memset runs between passes.
+#pragma once
+
+#include "sort_common.cuh"
+
+namespace gb300
+{
+
+__device__ __forceinline__ void named_barrier_256()
+{
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+}
+
+// Exclusive prefix over the 256 digit slots held by threads [0, 256) (one value per
+// thread). `scratch` holds 8 words. Must be called by exactly threads [0, 256).
+__device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch)
+{
+  const int tid  = threadIdx.x;
+  const int lane = tid & 31;
+  const int w    = tid >> 5;
+  uint32_t x     = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+    {
+      x += y;
+    }
+  }
+  if (lane == 31)
+  {
+    scratch[w] = x;
+  }
+  named_barrier_256();
+  uint32_t pre = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+  {
+    pre += (j < w) ? scratch[j] : 0u;
+  }
+  return pre + x - v;
+}
+
+// Stable rank of one warp's keys: in round i lane l holds the key at warp-local index
+// i*32+l, so (round, lane) order is source order. rank[i] = number of earlier keys of
+// the warp with the same digit. Per-warp digit counters live in whist_w[RADIX_DIGITS].
+template <class U, bool FP, int ITEMS>
+__device__ __forceinline__ void warp_rank(
+  const U (&keys)[ITEMS], uint32_t (&rank)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
+{
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t d     = extract_digit<U, FP>(keys[i], bit, dmask);
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t below = __popc(peers & lt);
+    const uint32_t base  = whist_w[d];
+    rank[i]              = base + below;
+    __syncwarp();
+    if (below == 0)
+    {
+      whist_w[d] = base + __popc(peers);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// init: zero a block of 32-bit words (the per-call control block)
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ void init_body(const InitParams& p)
+{
+  for (unsigned long long i = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; i < p.num_words;
+       i += (unsigned long long) gridDim.x * blockDim.x)
+  {
+    p.words[i] = 0u;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// histogram: counts of every pass's digit in one read; the last CTA writes the exclusive
+// prefix (global digit bases) of portion 0 for every pass. Also clears pass 0's look-back.
+// ---------------------------------------------------------------------------------------
+template <int KB, bool FP, int TPB>
+__device__ __forceinline__ void histogram_body(const HistogramParams& p)
+{
+  using U          = typename uint_of<KB>::type;
+  constexpr int R  = RADIX_DIGITS;
+  constexpr int VEC = 16 / KB;
+  __shared__ uint32_t sh[MAX_PASSES * R];
+  __shared__ uint32_t last_flag;
+
+  const int tid = threadIdx.x;
+  for (int i = tid; i < MAX_PASSES * R; i += TPB)
+  {
+    sh[i] = 0;
+  }
+  __syncthreads();
+
+  int shift[MAX_PASSES];
+  uint32_t mask[MAX_PASSES];
+#pragma unroll
+  for (int q = 0; q < MAX_PASSES; ++q)
+  {
+    const int b  = p.begin_bit + q * RADIX_BITS;
+    const int nb = min(RADIX_BITS, p.end_bit - b);
+    shift[q]     = b;
+    mask[q]      = (q < p.num_passes) ? ((1u << nb) - 1u) : 0u;
+  }
+
+  auto count_key = [&](U raw) {
+    const U t = encode_key<U>(raw, p.codec);
+#pragma unroll
+    for (int q = 0; q < MAX_PASSES; ++q)
+    {
+      if (q < p.num_passes)
+      {
+        atomicAdd(&sh[q * R + extract_digit<U, FP>(t, shift[q], mask[q])], 1u);
+      }
+    }
+  };
+
+  const U* keys             = static_cast<const U*>(p.keys);
+  const unsigned long long n = p.num_items;
+  // scalar head up to 16-byte alignment, vector body, scalar tail
+  const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
+  unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
+  if (head > n)
+  {
+    head = n;
+  }
+  const unsigned long long nvec = (n - head) / VEC;
+  const unsigned long long body_end = head + nvec * VEC;
+  if (blockIdx.x == 0)
+  {
+    for (unsigned long long i = tid; i < head; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+    for (unsigned long long i = body_end + tid; i < n; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+  }
+  const uint4* vkeys = reinterpret_cast<const uint4*>(keys + head);
+  for (unsigned long long v = blockIdx.x * (unsigned long long) TPB + tid; v < nvec;
+       v += (unsigned long long) gridDim.x * TPB)
+  {
+    const uint4 w = __ldcs(vkeys + v);
+    U k[VEC];
+    memcpy(k, &w, 16);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+    {
+      count_key(k[j]);
+    }
+  }
+
+  // clear the look-back buffer of pass 0
+  for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < p.lookback_words;
+       i += (unsigned long long) gridDim.x * TPB)
+  {
+    p.lookback_clear[i] = 0u;
+  }
+
+  __syncthreads();
+  for (int i = tid; i < p.num_passes * R; i += TPB)
+  {
+    if (sh[i] != 0)
+    {
+      atomicAdd(&p.ctrl->counts[i], (unsigned long long) sh[i]);
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0)
+  {
+    last_flag = (atomicAdd(&p.ctrl->hist_done, 1u) == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (last_flag == 0)
+  {
+    return;
+  }
+  __threadfence();
+  // one warp per pass: lane l owns digits [8l, 8l+8)
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+  if (warp < p.num_passes)
+  {
+    unsigned long long c[8];
+    unsigned long long s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+    {
+      c[j] = __ldcg(&p.ctrl->counts[warp * R + lane * 8 + j]);
+      s += c[j];
+    }
+    unsigned long long x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o)
+      {
+        x += y;
+      }
+    }
+    unsigned long long run = x - s;
+    unsigned long long* out = p.bins + (size_t) warp * p.num_portions * R;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+    {
+      out[lane * 8 + j] = run;
+      run += c[j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// onesweep: one stable digit pass over one portion
+// ---------------------------------------------------------------------------------------
+template <int KB, int VB, int TPB, int ITEMS>
+struct OnesweepSmem
+{
+  using U              = typename uint_of<KB>::type;
+  using V              = typename value_word<VB>::type;
+  static constexpr int NW   = TPB / 32;
+  static constexpr int TILE = TPB * ITEMS;
+  static constexpr size_t whist_off  = 0;
+  static constexpr size_t gdelta_off = whist_off + sizeof(uint32_t) * NW * RADIX_DIGITS;
+  static constexpr size_t misc_off   = gdelta_off + sizeof(long long) * RADIX_DIGITS;
+  static constexpr size_t kstage_off = misc_off + 128;
+  static constexpr size_t vstage_off = kstage_off + ((sizeof(U) * TILE + 15) / 16) * 16;
+  static constexpr size_t bytes      = vstage_off + (VB > 0 ? sizeof(V) * TILE : 0);
+};
+
+template <int KB, int VB, bool FP, int TPB, int ITEMS>
+__device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
+{
+  using L              = OnesweepSmem<KB, VB, TPB, ITEMS>;
+  using U              = typename L::U;
+  using V              = typename L::V;
+  constexpr int NW     = L::NW;
+  constexpr int TILE   = L::TILE;
+  constexpr int R      = RADIX_DIGITS;
+  static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
+  long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
+  uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);
+  U* kstage         = reinterpret_cast<U*>(smem + L::kstage_off);
+  V* vstage         = reinterpret_cast<V*>(smem + L::vstage_off);
+
+  const int tid  = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+
+  if (tid == 0)
+  {
+    misc[0] = atomicAdd(p.tile_counter, 1u);
+  }
+  for (int i = tid; i < NW * R; i += TPB)
+  {
+    whist[i] = 0;
+  }
+  __syncthreads();
+
+  const uint32_t tile       = misc[0];
+  const uint32_t tile_first = tile * TILE;
+  const uint32_t valid      = min(uint32_t(TILE), p.portion_items - tile_first);
+  const bool full           = valid == uint32_t(TILE);
+  const int bit             = p.current_bit;
+  const uint32_t dmask      = (1u << p.num_bits) - 1u;
+
+  // ---- load (warp-striped, coalesced) ----
+  const U* kin   = static_cast<const U*>(p.keys_in) + tile_first;
+  const int wofs = warp * ITEMS * 32 + lane;
+  U keys[ITEMS];
+  if (full)
+  {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      keys[i] = __ldcs(kin + wofs + i * 32);
+    }
+    if (p.encode_in)
+    {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        keys[i] = encode_key<U>(keys[i], p.codec);
+      }
+    }
+  }
+  else
+  {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      const uint32_t idx = wofs + i * 32;
+      U k                = U(~U(0));
+      if (idx < valid)
+      {
+        k = kin[idx];
+        if (p.encode_in)
+        {
+          k = encode_key<U>(k, p.codec);
+        }
+      }
+      keys[i] = k;
+    }
+  }
+
+  // ---- stable in-tile rank ----
+  uint32_t rank[ITEMS];
+  warp_rank<U, FP, ITEMS>(keys, rank, whist + warp * R, bit, dmask);
+  __syncthreads();
+
+  // ---- per-digit totals, publish, tile-local digit starts ----
+  uint32_t total = 0;
+  uint32_t tstart = 0;
+  uint32_t* lb_row = p.lookback + (size_t) (p.tile_row_base + tile) * R;
+  if (tid < R)
+  {
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+    {
+      const uint32_t c  = whist[w * R + tid];
+      whist[w * R + tid] = total;
+      total += c;
+    }
+    store_status(lb_row + tid, (tile == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+    tstart = digit_exclusive_scan(total, misc + 8);
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+    {
+      whist[w * R + tid] += tstart;
+    }
+  }
+  __syncthreads();
+
+  // ---- decoupled look-back (threads [0, 256), one digit each) ----
+  if (tid < R)
+  {
+    uint32_t excl = 0;
+    bool failed   = false;
+    if (tile > 0)
+    {
+      for (int j = int(tile) - 1; j >= 0; --j)
+      {
+        const uint32_t v = wait_status(p.lookback + (size_t) (p.tile_row_base + j) * R + tid);
+        const uint32_t f = v & LB_FLAGS;
+        if (f == LB_ERROR)
+        {
+          failed = true;
+          break;
+        }
+        excl += v & LB_VALUE;
+        if (f == LB_INCLUSIVE)
+        {
+          break;
+        }
+      }
+      store_status(lb_row + tid, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+      if (failed)
+      {
+        atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
+      }
+    }
+    if (p.lookback_next != nullptr)
+    {
+      p.lookback_next[(size_t) (p.tile_row_base + tile) * R + tid] = 0u;
+    }
+    const unsigned long long base = p.bins[tid] + excl;
+    gdelta[tid]                   = (long long) base - (long long) tstart;
+    if (p.bins_next != nullptr && tile == p.portion_tiles - 1)
+    {
+      p.bins_next[tid] = base + total;
+    }
+  }
+
+  // ---- scatter keys into the digit-sorted staging tile ----
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t d   = extract_digit<U, FP>(keys[i], bit, dmask);
+    const uint32_t pos = whist[warp * R + d] + rank[i];
+    kstage[pos]        = keys[i];
+    rank[i]            = pos;
+  }
+
+  V vals[VB > 0 ? ITEMS : 1];
+  if constexpr (VB > 0)
+  {
+    const V* vin = static_cast<const V*>(p.values_in) + tile_first;
+    if (full)
+    {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        vals[i] = __ldcs(vin + wofs + i * 32);
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        const uint32_t idx = wofs + i * 32;
+        if (idx < valid)
+        {
+          vals[i] = vin[idx];
+        }
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- write keys: consecutive staging slots of one digit go to consecutive outputs ----
+  U* kout = static_cast<U*>(p.keys_out);
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j)
+  {
+    const uint32_t s = j * TPB + tid;
+    if (full || s < valid)
+    {
+      const U k          = kstage[s];
+      const uint32_t d   = extract_digit<U, FP>(k, bit, dmask);
+      const long long g  = gdelta[d] + (long long) s;
+      __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+    }
+  }
+
+  if constexpr (VB > 0)
+  {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      vstage[rank[i]] = vals[i];
+    }
+    __syncthreads();
+    V* vout = static_cast<V*>(p.values_out);
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j)
+    {
+      const uint32_t s = j * TPB + tid;
+      if (full || s < valid)
+      {
+        const uint32_t d  = extract_digit<U, FP>(kstage[s], bit, dmask);
+        const long long g = gdelta[d] + (long long) s;
+        __stcs(vout + g, vstage[s]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// single tile: the whole LSD sort of <= TPB*ITEMS keys inside one CTA
+// ---------------------------------------------------------------------------------------
+template <int KB, int TPB, int ITEMS>
+struct SingleTileSmem
+{
+  using U              = typename uint_of<KB>::type;
+  static constexpr int NW   = TPB / 32;
+  static constexpr int TILE = TPB * ITEMS;
+  static constexpr size_t whist_off = 0;
+  static constexpr size_t misc_off  = whist_off + sizeof(uint32_t) * NW * RADIX_DIGITS;
+  static constexpr size_t kbuf_off  = misc_off + 128;
+  static constexpr size_t ibuf_off  = kbuf_off + ((2 * sizeof(U) * TILE + 15) / 16) * 16;
+  static constexpr size_t bytes     = ibuf_off + 2 * sizeof(uint16_t) * TILE;
+};
+
+template <int KB, int VB, bool FP, int TPB, int ITEMS>
+__device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
+{
+  using L            = SingleTileSmem<KB, TPB, ITEMS>;
+  using U            = typename L::U;
+  using V            = typename value_word<VB>::type;
+  constexpr int NW   = L::NW;
+  constexpr int TILE = L::TILE;
+  constexpr int R    = RADIX_DIGITS;
+  static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
+  static_assert(TILE <= 65536, "16-bit source indices");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* whist = reinterpret_cast<uint32_t*>(smem + L::whist_off);
+  uint32_t* misc  = reinterpret_cast<uint32_t*>(smem + L::misc_off);
+  U* kbuf         = reinterpret_cast<U*>(smem + L::kbuf_off);
+  uint16_t* ibuf  = reinterpret_cast<uint16_t*>(smem + L::ibuf_off);
+
+  const int tid    = threadIdx.x;
+  const int lane   = tid & 31;
+  const int warp   = tid >> 5;
+  const uint32_t n = p.num_items;
+  const U* kin     = static_cast<const U*>(p.keys_in);
+
+  for (int s = tid; s < TILE; s += TPB)
+  {
+    kbuf[s] = (uint32_t(s) < n) ? encode_key<U>(kin[s], p.codec) : U(~U(0));
+    ibuf[s] = uint16_t(s);
+  }
+
+  int cur = 0;
+  for (int bit = p.begin_bit; bit < p.end_bit; bit += RADIX_BITS)
+  {
+    const uint32_t dmask = (1u << min(RADIX_BITS, p.end_bit - bit)) - 1u;
+    for (int i = tid; i < NW * R; i += TPB)
+    {
+      whist[i] = 0;
+    }
+    __syncthreads();
+
+    const U* src       = kbuf + cur * TILE;
+    U* dst             = kbuf + (cur ^ 1) * TILE;
+    const uint16_t* is = ibuf + cur * TILE;
+    uint16_t* id       = ibuf + (cur ^ 1) * TILE;
+    const int wofs     = warp * ITEMS * 32 + lane;
+
+    U keys[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      keys[i] = src[wofs + i * 32];
+    }
+    uint32_t rank[ITEMS];
+    warp_rank<U, FP, ITEMS>(keys, rank, whist + warp * R, bit, dmask);
+    __syncthreads();
+    if (tid < R)
+    {
+      uint32_t total = 0;
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+      {
+        const uint32_t c  = whist[w * R + tid];
+        whist[w * R + tid] = total;
+        total += c;
+      }
+      const uint32_t tstart = digit_exclusive_scan(total, misc + 8);
+#pragma unroll
+      for (int w = 0; w < NW; ++w)
+      {
+        whist[w * R + tid] += tstart;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      const uint32_t d   = extract_digit<U, FP>(keys[i], bit, dmask);
+      const uint32_t pos = whist[warp * R + d] + rank[i];
+      dst[pos]           = keys[i];
+      id[pos]            = is[wofs + i * 32];
+    }
+    __syncthreads();
+    cur ^= 1;
+  }
+
+  U* kout             = static_cast<U*>(p.keys_out);
+  const U* kfin       = kbuf + cur * TILE;
+  const uint16_t* ifin = ibuf + cur * TILE;
+  for (uint32_t s = tid; s < n; s += TPB)
+  {
+    kout[s] = decode_key<U>(kfin[s], p.codec);
+    if constexpr (VB > 0)
+    {
+      static_cast<V*>(p.values_out)[s] = static_cast<const V*>(p.values_in)[ifin[s]];
+    }
+  }
+}
+
+} // namespace gb300

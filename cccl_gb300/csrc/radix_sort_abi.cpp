@@ -1,0 +1,518 @@
+// C ABI of the plain radix sort: cccl_device_radix_sort_{build,build_ex,compile,load,
+// link_ltoir,serialize,deserialize,cleanup} and the run entry cccl_device_radix_sort.
+//
+// Reference interface: c/parallel/include/cccl/c/radix_sort.h:27-143, implemented in
+// c/parallel/src/radix_sort.cu (compile :221-472, load :474-539, run :582-698,
+// cleanup :730-770, serialize/deserialize :816-947). The host dispatch follows CUB's
+// onesweep driver (cub/cub/device/dispatch/dispatch_radix_sort.cuh:1698-1948) and its
+// special cases (:1950-2003): empty input, begin_bit == end_bit, single tile.
+#include <cccl/c/radix_sort.h>
+#include <cccl/c/serialization.h>
+
+#include <algorithm>
+#include <memory>
+
+#include "abi_common.h"
+#include "radix_plan.h"
+#include "sort_policy.h"
+
+using namespace gb300;
+
+namespace
+{
+
+constexpr uint32_t POLICY_MAGIC = 0x52425047u; // "GPBR"
+
+bool is_keys_only(const cccl_iterator_t& values)
+{
+  return values.type == CCCL_POINTER && values.state == nullptr;
+}
+
+bool has_decomposer(const cccl_op_t& op)
+{
+  return op.name != nullptr && op.name[0] != '\0';
+}
+
+std::string suffix(int kind)
+{
+  return kind == KIND_FLOAT ? "f" : "i";
+}
+
+void free_names(cccl_device_radix_sort_build_result_t* b)
+{
+  for (char** p :
+       {&b->single_tile_kernel_lowered_name,
+        &b->upsweep_kernel_lowered_name,
+        &b->alt_upsweep_kernel_lowered_name,
+        &b->scan_bins_kernel_lowered_name,
+        &b->downsweep_kernel_lowered_name,
+        &b->alt_downsweep_kernel_lowered_name,
+        &b->histogram_kernel_lowered_name,
+        &b->exclusive_sum_kernel_lowered_name,
+        &b->init_bins_and_counters_kernel_lowered_name,
+        &b->init_lookback_kernel_lowered_name,
+        &b->onesweep_kernel_lowered_name})
+  {
+    delete[] *p;
+    *p = nullptr;
+  }
+}
+
+const RadixPolicy& policy_of(const cccl_device_radix_sort_build_result_t& b)
+{
+  if (b.runtime_policy == nullptr || b.runtime_policy_size != sizeof(RadixPolicy)
+      || static_cast<const RadixPolicy*>(b.runtime_policy)->magic != POLICY_MAGIC)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "build result has no valid runtime policy");
+  }
+  return *static_cast<const RadixPolicy*>(b.runtime_policy);
+}
+
+} // namespace
+
+extern "C" {
+
+CCCL_C_API void cccl_serialization_buffer_free(void* buf)
+{
+  std::free(buf);
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_compile(
+  cccl_device_radix_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t input_keys_it,
+  cccl_iterator_t input_values_it,
+  cccl_op_t decomposer,
+  const char* /*decomposer_return_type*/,
+  int cc_major,
+  int cc_minor,
+  const char* /*cub_path*/,
+  const char* /*thrust_path*/,
+  const char* /*libcudacxx_path*/,
+  const char* /*ctk_path*/,
+  cccl_build_config* /*config*/)
+try
+{
+  if (build == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (sort_order != CCCL_ASCENDING && sort_order != CCCL_DESCENDING)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (has_decomposer(decomposer))
+  {
+    printf("\nERROR in cccl_device_radix_sort_compile(): custom key decomposers are not supported\n");
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  if (cc_major * 10 + cc_minor != 103)
+  {
+    printf("\nERROR in cccl_device_radix_sort_compile(): kernels are built for sm_103a only (requested %d.%d)\n",
+           cc_major,
+           cc_minor);
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  int kind = 0, key_bytes = 0;
+  if (!key_kind_of(input_keys_it.value_type.type, kind, key_bytes)
+      || input_keys_it.value_type.size != size_t(key_bytes))
+  {
+    printf("\nERROR in cccl_device_radix_sort_compile(): unsupported key type\n");
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  const bool keys_only    = is_keys_only(input_values_it);
+  const size_t value_size = keys_only ? 0 : input_values_it.value_type.size;
+  if (!supported_value_bytes(value_size))
+  {
+    printf("\nERROR in cccl_device_radix_sort_compile(): value size %zu is not supported\n", value_size);
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+
+  const image_ref img = radix_image(key_bytes);
+  std::unique_ptr<char[]> payload(new char[img.size]);
+  std::memcpy(payload.get(), img.data, img.size);
+
+  auto* pol        = static_cast<RadixPolicy*>(std::malloc(sizeof(RadixPolicy)));
+  if (pol == nullptr)
+  {
+    return CUDA_ERROR_OUT_OF_MEMORY;
+  }
+  *pol = make_radix_policy(key_bytes, int(value_size), kind);
+  pol->magic = POLICY_MAGIC;
+
+  const std::string s   = suffix(kind);
+  const std::string kv  = "k" + std::to_string(key_bytes) + "_v" + std::to_string(value_size) + "_" + s;
+  const std::string one = "gb300_onesweep_" + kv;
+  const std::string st  = "gb300_single_tile_" + kv;
+  const std::string his = "gb300_histogram_k" + std::to_string(key_bytes) + "_" + s;
+  const std::string ini = "gb300_init";
+
+  cccl_device_radix_sort_build_result_t r{};
+  r.cc                   = cc_major * 10 + cc_minor;
+  r.payload              = payload.release();
+  r.payload_size         = img.size;
+  r.payload_kind         = CCCL_PAYLOAD_CUBIN;
+  r.key_type             = input_keys_it.value_type;
+  r.value_type           = input_values_it.value_type;
+  r.order                = sort_order;
+  r.runtime_policy       = pol;
+  r.runtime_policy_size  = sizeof(RadixPolicy);
+  r.single_tile_kernel_lowered_name            = dup_cstr(st);
+  r.upsweep_kernel_lowered_name                = dup_cstr(his);
+  r.alt_upsweep_kernel_lowered_name            = dup_cstr(his);
+  r.scan_bins_kernel_lowered_name              = dup_cstr(his);
+  r.downsweep_kernel_lowered_name              = dup_cstr(one);
+  r.alt_downsweep_kernel_lowered_name          = dup_cstr(one);
+  r.histogram_kernel_lowered_name              = dup_cstr(his);
+  r.exclusive_sum_kernel_lowered_name          = dup_cstr(his);
+  r.init_bins_and_counters_kernel_lowered_name = dup_cstr(ini);
+  r.init_lookback_kernel_lowered_name          = dup_cstr(ini);
+  r.onesweep_kernel_lowered_name               = dup_cstr(one);
+  *build                                       = r;
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_radix_sort_compile", e);
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_load(cccl_device_radix_sort_build_result_t* build)
+try
+{
+  auto invalid = [](const char* n) {
+    return n == nullptr || n[0] == '\0';
+  };
+  if (build == nullptr || build->payload == nullptr || build->payload_size == 0
+      || build->payload_kind != CCCL_PAYLOAD_CUBIN || invalid(build->single_tile_kernel_lowered_name)
+      || invalid(build->upsweep_kernel_lowered_name) || invalid(build->alt_upsweep_kernel_lowered_name)
+      || invalid(build->scan_bins_kernel_lowered_name) || invalid(build->downsweep_kernel_lowered_name)
+      || invalid(build->alt_downsweep_kernel_lowered_name) || invalid(build->histogram_kernel_lowered_name)
+      || invalid(build->exclusive_sum_kernel_lowered_name)
+      || invalid(build->init_bins_and_counters_kernel_lowered_name)
+      || invalid(build->init_lookback_kernel_lowered_name) || invalid(build->onesweep_kernel_lowered_name))
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  const CUresult st = cuLibraryLoadData(&build->library, build->payload, nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (st != CUDA_SUCCESS)
+  {
+    return st;
+  }
+  try
+  {
+    auto get = [&](CUkernel* k, const char* name) {
+      check(cuLibraryGetKernel(k, build->library, name), name);
+    };
+    get(&build->single_tile_kernel, build->single_tile_kernel_lowered_name);
+    get(&build->upsweep_kernel, build->upsweep_kernel_lowered_name);
+    get(&build->alt_upsweep_kernel, build->alt_upsweep_kernel_lowered_name);
+    get(&build->scan_bins_kernel, build->scan_bins_kernel_lowered_name);
+    get(&build->downsweep_kernel, build->downsweep_kernel_lowered_name);
+    get(&build->alt_downsweep_kernel, build->alt_downsweep_kernel_lowered_name);
+    get(&build->histogram_kernel, build->histogram_kernel_lowered_name);
+    get(&build->exclusive_sum_kernel, build->exclusive_sum_kernel_lowered_name);
+    get(&build->init_bins_and_counters_kernel, build->init_bins_and_counters_kernel_lowered_name);
+    get(&build->init_lookback_kernel, build->init_lookback_kernel_lowered_name);
+    get(&build->onesweep_kernel, build->onesweep_kernel_lowered_name);
+  }
+  catch (...)
+  {
+    cuLibraryUnload(build->library);
+    build->library = nullptr;
+    throw;
+  }
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_radix_sort_load", e);
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_build_ex(
+  cccl_device_radix_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t input_keys_it,
+  cccl_iterator_t input_values_it,
+  cccl_op_t decomposer,
+  const char* decomposer_return_type,
+  int cc_major,
+  int cc_minor,
+  const char* cub_path,
+  const char* thrust_path,
+  const char* libcudacxx_path,
+  const char* ctk_path,
+  cccl_build_config* config)
+{
+  CUresult r = cccl_device_radix_sort_compile(
+    build,
+    sort_order,
+    input_keys_it,
+    input_values_it,
+    decomposer,
+    decomposer_return_type,
+    cc_major,
+    cc_minor,
+    cub_path,
+    thrust_path,
+    libcudacxx_path,
+    ctk_path,
+    config);
+  if (r != CUDA_SUCCESS)
+  {
+    return r;
+  }
+  r = cccl_device_radix_sort_load(build);
+  if (r != CUDA_SUCCESS)
+  {
+    cccl_device_radix_sort_cleanup(build);
+  }
+  return r;
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_build(
+  cccl_device_radix_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t input_keys_it,
+  cccl_iterator_t input_values_it,
+  cccl_op_t decomposer,
+  const char* decomposer_return_type,
+  int cc_major,
+  int cc_minor,
+  const char* cub_path,
+  const char* thrust_path,
+  const char* libcudacxx_path,
+  const char* ctk_path)
+{
+  return cccl_device_radix_sort_build_ex(
+    build,
+    sort_order,
+    input_keys_it,
+    input_values_it,
+    decomposer,
+    decomposer_return_type,
+    cc_major,
+    cc_minor,
+    cub_path,
+    thrust_path,
+    libcudacxx_path,
+    ctk_path,
+    nullptr);
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort(
+  cccl_device_radix_sort_build_result_t build,
+  void* d_temp_storage,
+  size_t* temp_storage_bytes,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_keys_out,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t d_values_out,
+  cccl_op_t decomposer,
+  uint64_t num_items,
+  int begin_bit,
+  int end_bit,
+  bool is_overwrite_okay,
+  int* selector,
+  CUstream stream)
+{
+  if (d_keys_in.type != CCCL_POINTER || d_keys_out.type != CCCL_POINTER || d_values_in.type != CCCL_POINTER
+      || d_values_out.type != CCCL_POINTER)
+  {
+    fflush(stderr);
+    printf("\nERROR in cccl_device_radix_sort(): radix sort input must be a pointer\n");
+    fflush(stdout);
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (temp_storage_bytes == nullptr || selector == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (has_decomposer(decomposer))
+  {
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  try
+  {
+    context_guard ctx;
+    const RadixPolicy& pol = policy_of(build);
+    if (build.library == nullptr || build.onesweep_kernel == nullptr)
+    {
+      return CUDA_ERROR_NOT_INITIALIZED;
+    }
+    RadixKernels ks{build.init_bins_and_counters_kernel,
+                    build.histogram_kernel,
+                    build.onesweep_kernel,
+                    build.single_tile_kernel};
+    RadixCall call{};
+    call.keys[0]          = d_keys_in.state;
+    call.keys[1]          = d_keys_out.state;
+    call.values[0]        = d_values_in.state;
+    call.values[1]        = d_values_out.state;
+    call.num_items        = num_items;
+    call.begin_bit        = begin_bit;
+    call.end_bit          = end_bit;
+    call.overwrite        = is_overwrite_okay;
+    call.descending       = build.order == CCCL_DESCENDING;
+    call.d_temp_storage   = d_temp_storage;
+    call.temp_storage_bytes = temp_storage_bytes;
+    call.stream           = stream;
+    int sel               = 0;
+    radix_sort_dispatch(pol, ks, call, &sel);
+    *selector = sel;
+    return CUDA_SUCCESS;
+  }
+  catch (const std::exception& e)
+  {
+    return report("cccl_device_radix_sort", e);
+  }
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_link_ltoir(
+  cccl_device_radix_sort_build_result_t* build, const void** input_blobs, const size_t* input_sizes, size_t num_inputs)
+{
+  // The payload is a finished cubin: there is no LTO-IR stage to link into.
+  (void) input_blobs;
+  (void) input_sizes;
+  (void) num_inputs;
+  if (build == nullptr || build->payload == nullptr || build->payload_size == 0
+      || build->payload_kind != CCCL_PAYLOAD_LTOIR)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  return CUDA_ERROR_NOT_SUPPORTED;
+}
+
+CCCL_C_API CUresult
+cccl_device_radix_sort_serialize(const cccl_device_radix_sort_build_result_t* b, void** out_buf, size_t* out_size)
+try
+{
+  if (b == nullptr || out_buf == nullptr || out_size == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (b->payload == nullptr || b->payload_size == 0 || b->runtime_policy == nullptr || b->runtime_policy_size == 0)
+  {
+    *out_buf  = nullptr;
+    *out_size = 0;
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  blob_writer w;
+  write_header(w, 7u /* CCCL_SERIALIZATION_ALGO_RADIX_SORT */, b->payload_kind, b->cc);
+  w.type_info(b->key_type);
+  w.type_info(b->value_type);
+  w.pod<uint32_t>(uint32_t(b->order));
+  w.blob(b->payload, b->payload_size);
+  w.blob(b->runtime_policy, b->runtime_policy_size);
+  w.cstr(b->single_tile_kernel_lowered_name);
+  w.cstr(b->upsweep_kernel_lowered_name);
+  w.cstr(b->alt_upsweep_kernel_lowered_name);
+  w.cstr(b->scan_bins_kernel_lowered_name);
+  w.cstr(b->downsweep_kernel_lowered_name);
+  w.cstr(b->alt_downsweep_kernel_lowered_name);
+  w.cstr(b->histogram_kernel_lowered_name);
+  w.cstr(b->exclusive_sum_kernel_lowered_name);
+  w.cstr(b->init_bins_and_counters_kernel_lowered_name);
+  w.cstr(b->init_lookback_kernel_lowered_name);
+  w.cstr(b->onesweep_kernel_lowered_name);
+  w.release(out_buf, out_size);
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_radix_sort_serialize", e);
+}
+
+CCCL_C_API CUresult
+cccl_device_radix_sort_deserialize(cccl_device_radix_sort_build_result_t* build, const void* buf, size_t size)
+try
+{
+  if (build == nullptr || buf == nullptr || size == 0)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  blob_reader rd{static_cast<const unsigned char*>(buf), size};
+  const blob_header h = read_header(rd, 7u);
+  cccl_device_radix_sort_build_result_t r{};
+  r.cc         = h.cc;
+  r.payload_kind = cccl_payload_kind_t(h.payload_kind);
+  r.key_type   = rd.type_info();
+  r.value_type = rd.type_info();
+  r.order      = cccl_sort_order_t(rd.pod<uint32_t>());
+  if (r.order != CCCL_ASCENDING && r.order != CCCL_DESCENDING)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: invalid sort order");
+  }
+  std::unique_ptr<char[]> payload(static_cast<char*>(rd.blob_new(&r.payload_size)));
+  if (r.payload_size == 0)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: empty payload");
+  }
+  size_t pol_size = 0;
+  std::unique_ptr<char[]> pol_bytes(static_cast<char*>(rd.blob_new(&pol_size)));
+  if (pol_size != sizeof(RadixPolicy))
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: policy size mismatch");
+  }
+  auto* pol = static_cast<RadixPolicy*>(std::malloc(sizeof(RadixPolicy)));
+  if (pol == nullptr)
+  {
+    return CUDA_ERROR_OUT_OF_MEMORY;
+  }
+  std::memcpy(pol, pol_bytes.get(), sizeof(RadixPolicy));
+  if (pol->magic != POLICY_MAGIC)
+  {
+    std::free(pol);
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: bad policy");
+  }
+  std::unique_ptr<char[]> names[11];
+  for (auto& n : names)
+  {
+    n.reset(rd.cstr_new());
+  }
+  r.payload                                    = payload.release();
+  r.runtime_policy                             = pol;
+  r.runtime_policy_size                        = sizeof(RadixPolicy);
+  r.single_tile_kernel_lowered_name            = names[0].release();
+  r.upsweep_kernel_lowered_name                = names[1].release();
+  r.alt_upsweep_kernel_lowered_name            = names[2].release();
+  r.scan_bins_kernel_lowered_name              = names[3].release();
+  r.downsweep_kernel_lowered_name              = names[4].release();
+  r.alt_downsweep_kernel_lowered_name          = names[5].release();
+  r.histogram_kernel_lowered_name              = names[6].release();
+  r.exclusive_sum_kernel_lowered_name          = names[7].release();
+  r.init_bins_and_counters_kernel_lowered_name = names[8].release();
+  r.init_lookback_kernel_lowered_name          = names[9].release();
+  r.onesweep_kernel_lowered_name               = names[10].release();
+  *build                                       = r;
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_radix_sort_deserialize", e);
+}
+
+CCCL_C_API CUresult cccl_device_radix_sort_cleanup(cccl_device_radix_sort_build_result_t* b)
+try
+{
+  if (b == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  delete[] static_cast<char*>(b->payload);
+  b->payload = nullptr;
+  std::free(b->runtime_policy);
+  b->runtime_policy = nullptr;
+  free_names(b);
+  if (b->library != nullptr)
+  {
+    check(cuLibraryUnload(b->library), "cuLibraryUnload");
+    b->library = nullptr;
+  }
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_radix_sort_cleanup", e);
+}
+
+} // extern "C"

@@ -1,0 +1,164 @@
+// Device-side building blocks shared by the sort kernels: key bit-ordering, digit
+// extraction, launch parameter blocks and the bounded look-back wait.
+//
+// Semantics follow CUB's radix sort exactly:
+//  * keys are mapped to an unsigned bit order before ranking (cub/cub/util_type.cuh:893-963
+//    Traits<T>::TwiddleIn/TwiddleOut), then bit-inverted for descending order
+//    (cub/cub/block/radix_rank_sort_operations.cuh:536-575 RadixSortTwiddle);
+//  * for floating-point keys the bit-ordered -0.0 is treated as +0.0 only when a digit is
+//    extracted (radix_rank_sort_operations.cuh:43-80, ShiftDigitExtractor::Digit :124-127),
+//    so +-0 compare equal, stay stable, and keep their own bit patterns in the output.
+#pragma once
+
+#include <cstdint>
+
+#include "sort_params.h"
+
+namespace gb300
+{
+
+template <int BYTES>
+struct uint_of;
+template <>
+struct uint_of<1>
+{
+  using type = uint8_t;
+};
+template <>
+struct uint_of<2>
+{
+  using type = uint16_t;
+};
+template <>
+struct uint_of<4>
+{
+  using type = uint32_t;
+};
+template <>
+struct uint_of<8>
+{
+  using type = unsigned long long;
+};
+
+// Opaque value payloads are moved as words of their own size.
+template <int BYTES>
+struct value_word
+{
+  using type = typename uint_of<BYTES>::type;
+};
+template <>
+struct value_word<16>
+{
+  using type = uint4;
+};
+template <>
+struct value_word<0>
+{
+  using type = uint32_t; // unused (keys-only)
+};
+
+template <class U>
+__device__ __forceinline__ constexpr U high_bit()
+{
+  return U(U(1) << (8 * sizeof(U) - 1));
+}
+
+// Forward map raw key bits -> sortable unsigned bits (order already applied).
+template <class U>
+__device__ __forceinline__ U encode_key(U x, const KeyCodec& c)
+{
+  return U(x ^ U((x & high_bit<U>()) ? c.fwd_neg : c.fwd_pos));
+}
+
+// Inverse map sortable bits -> raw key bits.
+template <class U>
+__device__ __forceinline__ U decode_key(U t, const KeyCodec& c)
+{
+  return U(t ^ U((t & high_bit<U>()) ? c.inv_set : c.inv_clr));
+}
+
+// Digit source: for floating-point keys the encoded -0.0 (0x7f..f in both orders) is
+// replaced by the encoded +0.0 pattern (0x80..0) before the shift.
+template <class U, bool FP>
+__device__ __forceinline__ U digit_source(U t)
+{
+  if constexpr (FP)
+  {
+    return (t == U(~high_bit<U>())) ? high_bit<U>() : t;
+  }
+  else
+  {
+    return t;
+  }
+}
+
+template <class U, bool FP>
+__device__ __forceinline__ uint32_t extract_digit(U t, int bit, uint32_t mask)
+{
+  return uint32_t(digit_source<U, FP>(t) >> bit) & mask;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint64_t global_timer_ns()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Look-back status word: bits 31..30 = flag, bits 29..0 = digit count.
+constexpr uint32_t LB_EMPTY     = 0u;
+constexpr uint32_t LB_PARTIAL   = 1u << 30;
+constexpr uint32_t LB_INCLUSIVE = 2u << 30;
+constexpr uint32_t LB_ERROR     = 3u << 30;
+constexpr uint32_t LB_FLAGS     = 3u << 30;
+constexpr uint32_t LB_VALUE     = (1u << 30) - 1;
+
+__device__ __forceinline__ uint32_t load_status(const uint32_t* p)
+{
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void store_status(uint32_t* p, uint32_t v)
+{
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Waits until the status word is non-empty. Gives up after LOOKBACK_TIMEOUT_NS and
+// returns LB_ERROR, so a stuck predecessor can never hang the GPU.
+__device__ __forceinline__ uint32_t wait_status(const uint32_t* p)
+{
+  uint32_t v = load_status(p);
+  if ((v & LB_FLAGS) != LB_EMPTY)
+  {
+    return v;
+  }
+  const uint64_t start = global_timer_ns();
+  uint32_t spins       = 0;
+  while (true)
+  {
+    v = load_status(p);
+    if ((v & LB_FLAGS) != LB_EMPTY)
+    {
+      return v;
+    }
+    if (++spins > 32)
+    {
+      __nanosleep(64);
+      if (global_timer_ns() - start > LOOKBACK_TIMEOUT_NS)
+      {
+        return LB_ERROR;
+      }
+    }
+  }
+}
+
+} // namespace gb300

@@ -1,0 +1,82 @@
+// Tile configuration of the plain-path kernels per key/value width: the single source
+// of truth for both the kernel instantiations and the host dispatcher (grid sizes,
+// dynamic shared memory, temp-storage layout). Plain C++, usable from host and device.
+//
+// The reference's equivalent is the sm_100 onesweep tuning
+// (cub/cub/device/dispatch/tuning/tuning_radix_sort.cuh:1743-1800): 384 threads and
+// 12..23 items per thread under a 48 KB static shared-memory cap. GB300 kernels here use
+// dynamic shared memory, so the staging tile is sized by registers, not by the 48 KB cap.
+#pragma once
+
+#include <cstddef>
+
+#if defined(__CUDACC__)
+#  define GB300_HD __host__ __device__
+#else
+#  define GB300_HD
+#endif
+
+namespace gb300
+{
+
+constexpr int ONESWEEP_TPB     = 384;
+constexpr int SINGLE_TILE_TPB  = 512;
+constexpr int SINGLE_TILE_ITEMS = 10;
+constexpr int HISTOGRAM_TPB    = 512;
+
+GB300_HD constexpr int onesweep_items(int kb, int vb)
+{
+  return vb >= 16 ? 8
+       : kb == 8  ? (vb == 0 ? 16 : 12)
+       : kb == 4  ? (vb == 0 ? 20 : vb <= 4 ? 16 : 12)
+                  : 16;
+}
+
+GB300_HD constexpr size_t round16(size_t x)
+{
+  return (x + 15) / 16 * 16;
+}
+
+GB300_HD constexpr size_t value_word_bytes(int vb)
+{
+  return vb == 0 ? 4 : size_t(vb);
+}
+
+// Dynamic shared memory of the onesweep kernel: per-warp digit counters, per-digit
+// global deltas, a misc block, the key staging tile and (pairs) the value staging tile.
+GB300_HD constexpr size_t onesweep_smem_bytes(int kb, int vb)
+{
+  return size_t(4) * (ONESWEEP_TPB / 32) * 256 + size_t(8) * 256 + 128
+       + round16(size_t(kb) * ONESWEEP_TPB * onesweep_items(kb, vb))
+       + (vb > 0 ? value_word_bytes(vb) * ONESWEEP_TPB * onesweep_items(kb, vb) : 0);
+}
+
+GB300_HD constexpr int single_tile_capacity()
+{
+  return SINGLE_TILE_TPB * SINGLE_TILE_ITEMS;
+}
+
+GB300_HD constexpr size_t single_tile_smem_bytes(int kb)
+{
+  return size_t(4) * (SINGLE_TILE_TPB / 32) * 256 + 128 + round16(size_t(2) * kb * single_tile_capacity())
+       + size_t(2) * 2 * single_tile_capacity();
+}
+
+// Largest input CUB sorts with its single-tile kernel (256 threads x 19 items scaled
+// by the dominant type size, tuning_radix_sort.cuh:1833-1841 and scale_reg_bound in
+// cub/cub/util_arch.cuh:128-139). Using the same cut keeps the returned DoubleBuffer
+// selector identical to CUB's.
+GB300_HD constexpr unsigned long long cub_single_tile_limit(int key_bytes, int value_bytes)
+{
+  const int dom   = key_bytes > value_bytes ? key_bytes : value_bytes;
+  const int items = (19 * 4 / (dom > 4 ? dom : 4)) > 1 ? (19 * 4 / (dom > 4 ? dom : 4)) : 1;
+  const int t     = ((48 * 1024 / (dom * items)) + 31) / 32 * 32;
+  const int tpb   = t < 256 ? t : 256;
+  return (unsigned long long) tpb * items;
+}
+
+static_assert(cub_single_tile_limit(4, 0) == 4864, "CUB single-tile cut, 4-byte keys");
+static_assert(cub_single_tile_limit(8, 4) == 2304, "CUB single-tile cut, 8-byte keys");
+static_assert(cub_single_tile_limit(4, 16) == 1024, "CUB single-tile cut, 16-byte values");
+
+} // namespace gb300

@@ -1,0 +1,127 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, exports every symbol
+the headers declare, and its compile / serialize / deserialize / cleanup / argument
+checks behave like the reference's (c/parallel/test/test_radix_sort.cpp:332-471)."""
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def lib(built_library):
+    from cccl_gb300 import _bindings as B
+
+    return B.load_library(allow_driver_stub=True)
+
+
+def header_symbols():
+    names = set()
+    for h in (ROOT / "include" / "cccl" / "c").glob("*.h"):
+        names |= set(re.findall(r"CCCL_C_API\s+(?:\w+\s+)*?(cccl_\w+)\s*\(", h.read_text()))
+        names |= set(re.findall(r"CCCL_C_API\s+CUresult\s*\n\s*(cccl_\w+)\s*\(", h.read_text()))
+    return names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from cccl_gb300 import _bindings as B
+
+    declared = header_symbols()
+    assert declared == set(B.EXPORTED_SYMBOLS)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def _compile(lib, key_type=None, value_type=None, order=0, cc=(10, 3), decomposer_name=None):
+    from cccl_gb300 import _bindings as B
+
+    key_type = key_type if key_type is not None else (B.UINT32, 4)
+    build = B.RadixSortBuildResult()
+    keys = B.pointer_iterator(0x1000, key_type[0], key_type[1])
+    vals = B.pointer_iterator(0x2000 if value_type else 0, *(value_type or (B.STORAGE, 4)))
+    op = B.Op()
+    if decomposer_name:
+        op.name = decomposer_name
+    rc = lib.cccl_device_radix_sort_compile(
+        C.byref(build), order, keys, vals, op, b"", cc[0], cc[1], None, None, None, None, None
+    )
+    return rc, build
+
+
+def test_compile_fills_build_result(lib):
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _compile(lib, (B.FLOAT32, 4), (B.UINT32, 4), order=B.DESCENDING)
+    assert rc == B.CUDA_SUCCESS
+    assert b.cc == 103 and b.payload and b.payload_size > 0 and b.payload_kind == B.PAYLOAD_CUBIN
+    assert b.runtime_policy and b.runtime_policy_size > 0 and b.order == B.DESCENDING
+    assert b.onesweep_kernel_lowered_name == b"gb300_onesweep_k4_v4_f"
+    assert b.histogram_kernel_lowered_name == b"gb300_histogram_k4_f"
+    for f, _ in B.RadixSortBuildResult._fields_:
+        if f.endswith("_lowered_name"):
+            assert getattr(b, f), f
+    assert not b.library and not b.onesweep_kernel  # nothing loaded before _load
+    assert lib.cccl_device_radix_sort_cleanup(C.byref(b)) == B.CUDA_SUCCESS
+
+
+def test_serialize_round_trip(lib):
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _compile(lib, (B.INT64, 8), (B.FLOAT64, 8))
+    assert rc == 0
+    buf, size = C.c_void_p(), C.c_size_t()
+    assert lib.cccl_device_radix_sort_serialize(C.byref(b), C.byref(buf), C.byref(size)) == 0
+    assert size.value > b.payload_size
+    b2 = B.RadixSortBuildResult()
+    assert lib.cccl_device_radix_sort_deserialize(C.byref(b2), buf, size) == 0
+    assert b2.payload_size == b.payload_size and b2.cc == b.cc and b2.order == b.order
+    assert C.string_at(b2.payload, b2.payload_size) == C.string_at(b.payload, b.payload_size)
+    assert b2.onesweep_kernel_lowered_name == b.onesweep_kernel_lowered_name
+    assert b2.key_type.type == B.INT64 and b2.value_type.size == 8
+    assert not b2.library
+    # a truncated or foreign blob is rejected and leaves the target untouched
+    b3 = B.RadixSortBuildResult()
+    assert lib.cccl_device_radix_sort_deserialize(C.byref(b3), buf, 10) != 0
+    assert not b3.payload
+    raw = bytearray(C.string_at(buf, size.value))
+    raw[8] = 8  # algorithm tag: segmented sort
+    assert lib.cccl_device_radix_sort_deserialize(C.byref(b3), bytes(raw), len(raw)) != 0
+    lib.cccl_serialization_buffer_free(buf)
+    for x in (b, b2):
+        assert lib.cccl_device_radix_sort_cleanup(C.byref(x)) == 0
+
+
+def test_compile_rejections(lib):
+    from cccl_gb300 import _bindings as B
+
+    assert _compile(lib, cc=(9, 0))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _compile(lib, decomposer_name=b"my_decomposer")[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _compile(lib, key_type=(B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _compile(lib, value_type=(B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _compile(lib, value_type=(B.STORAGE, 16))[0] == B.CUDA_SUCCESS
+    assert lib.cccl_device_radix_sort_cleanup(None) == B.CUDA_ERROR_INVALID_VALUE
+    assert lib.cccl_device_radix_sort_load(None) == B.CUDA_ERROR_INVALID_VALUE
+
+
+def test_run_rejects_non_pointer_iterators(lib):
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _compile(lib)
+    it = B.pointer_iterator(0x1000, B.UINT32, 4)
+    bad = B.pointer_iterator(0x1000, B.UINT32, 4)
+    bad.type = B.ITERATOR
+    nbytes, sel = C.c_size_t(0), C.c_int(-1)
+    r = lib.cccl_device_radix_sort(b, None, C.byref(nbytes), bad, it, it, it, B.Op(), 16, 0, 32, False, C.byref(sel), None)
+    assert r == B.CUDA_ERROR_UNKNOWN
+    lib.cccl_device_radix_sort_cleanup(C.byref(b))
+
+
+def test_link_ltoir_has_nothing_to_link(lib):
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _compile(lib)
+    assert lib.cccl_device_radix_sort_link_ltoir(C.byref(b), None, None, 0) == B.CUDA_ERROR_INVALID_VALUE
+    lib.cccl_device_radix_sort_cleanup(C.byref(b))
