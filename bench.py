@@ -1,0 +1,441 @@
+"""Benchmark of the sort engine on one GB300 (or N replicas).
+
+Workload (one "step"): cub::DeviceRadixSort::SortPairs of 2^28 uint64 keys (uniform over
+the full 64-bit range, i.e. 64 bits of entropy) with uint32 values (value = original
+index), ascending, begin_bit 0 / end_bit 64, through the library's C ABI
+(cccl_device_radix_sort). Inputs (3.2 GB) exceed the 129 MB L2, so no flush is needed
+between steps. Variants of the same configuration (entropy 43.7/33.4/13.0-bit style
+AND-reduced keys, a constant key, descending, begin_bit 8 / end_bit 40) and the 2^28
+uint32 keys-only roofline row are reported under "variants".
+
+Metric: sorted keys per second (higher is better); roofline on HBM with algorithmic bytes
+= passes x N x 2 x (key + value bytes).
+
+--impl reference times the reference library's CPU sort (thrust::sort_by_key on its
+OpenMP backend, from the toolkit's CCCL headers) on a bounded sample of the workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+N_LOG2 = 28
+METRIC = "sorted keys/s (SortPairs 2^28 u64 keys + u32 values, 1 GB300)"
+UNIT = "keys/s"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return rank, world
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_inputs(torch, n, key_dtype, ands=1, constant=False, seed=1):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    if key_dtype == "u64":
+        def draw():
+            return torch.randint(-(2**63), 2**63 - 1, (n,), device="cuda", dtype=torch.int64, generator=g)
+        k = draw()
+        for _ in range(ands - 1):
+            k &= draw()
+        if constant:
+            k.fill_(0x0123456789ABCDEF)
+        k = k.view(torch.uint64) if hasattr(torch, "uint64") else k  # same storage, sorted as uint64
+    else:  # u32
+        k = torch.randint(-(2**31), 2**31 - 1, (n,), device="cuda", dtype=torch.int32, generator=g)
+        k = k.view(torch.uint32) if hasattr(torch, "uint32") else k
+    return k
+
+
+class Sorter:
+    """One configured sort through the C ABI with preallocated buffers."""
+
+    def __init__(self, torch, keys, with_values, descending=False, begin_bit=0, end_bit=None):
+        from cccl_gb300 import SortOrder, make_radix_sort
+
+        self.torch = torch
+        n = keys.numel()
+        self.n = n
+        self.ki = keys
+        self.ko = torch.empty_like(keys)
+        self.vi = torch.arange(n, device="cuda", dtype=torch.int32) if with_values else None
+        self.vo = torch.empty_like(self.vi) if with_values else None
+        self.begin_bit = begin_bit
+        self.end_bit = end_bit if end_bit is not None else keys.element_size() * 8
+        self.args = dict(d_in_keys=self.ki, d_out_keys=self.ko, d_in_values=self.vi, d_out_values=self.vo)
+        self.sorter = make_radix_sort(order=SortOrder.DESCENDING if descending else SortOrder.ASCENDING, **self.args)
+        nb = self.sorter(temp_storage=None, num_items=n, begin_bit=self.begin_bit, end_bit=self.end_bit, **self.args)
+        self.temp = torch.empty(nb, dtype=torch.uint8, device="cuda")
+        self.key_bytes = keys.element_size()
+        self.value_bytes = 4 if with_values else 0
+        self.passes = -(-(self.end_bit - self.begin_bit) // 8)
+
+    def run(self, stream=None):
+        self.sorter(temp_storage=self.temp, num_items=self.n, begin_bit=self.begin_bit, end_bit=self.end_bit,
+                    stream=stream, **self.args)
+
+    def algorithmic_bytes(self):
+        return self.passes * self.n * 2 * (self.key_bytes + self.value_bytes)
+
+
+def time_steps(torch, fn, steps, warmup, barrier):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / steps  # ms per step
+
+
+def kernel_times(torch, sorter, steps):
+    """Per-role kernel durations (ms), from CUDA events recorded on the launching stream
+    by the library's launch observer."""
+    from cccl_gb300 import _bindings as B
+
+    lib = B.load_library()
+    stream = torch.cuda.current_stream()
+    records = []
+
+    def observer(user, role, phase, s):
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        records.append((role.decode(), phase, ev))
+
+    cb = B.LAUNCH_OBSERVER(observer)
+    lib.cccl_gb300_set_launch_observer(cb, None)
+    try:
+        for _ in range(steps):
+            sorter.run()
+        torch.cuda.synchronize()
+    finally:
+        lib.cccl_gb300_set_launch_observer(B.LAUNCH_OBSERVER(0), None)
+    out, count = {}, {}
+    open_ev = {}
+    for role, phase, ev in records:
+        if phase == 0:
+            open_ev[role] = ev
+        else:
+            out.setdefault(role, []).append(open_ev.pop(role).elapsed_time(ev))
+            count[role] = count.get(role, 0) + 1
+    launches_per_step = sum(count.values()) // steps
+    return {r: statistics.mean(v) for r, v in out.items()}, launches_per_step
+
+
+def cpu_reference_sort(n_sample, threads, key_dtype="u64", with_values=True, reps=3):
+    """thrust::sort_by_key on the OpenMP backend over a bounded sample (keys/s)."""
+    import numpy as np
+
+    lib = C.CDLL(str(ROOT / "oracle" / "libthrust_omp.so"))
+    lib.thrust_omp_sort.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64, C.c_int, C.c_int]
+    lib.thrust_omp_sort.restype = C.c_int
+    rng = np.random.default_rng(7)
+    dt = np.uint64 if key_dtype == "u64" else np.uint32
+    base = rng.integers(0, np.iinfo(dt).max, size=n_sample, dtype=dt, endpoint=True)
+    code = 7 if key_dtype == "u64" else 6
+    times = []
+    for _ in range(reps):
+        k = base.copy()
+        v = np.arange(n_sample, dtype=np.uint32) if with_values else None
+        t0 = time.perf_counter()
+        rc = lib.thrust_omp_sort(code, k.ctypes.data, 4 if with_values else 0, v.ctypes.data if v is not None else None,
+                                 n_sample, 0, threads)
+        times.append(time.perf_counter() - t0)
+        assert rc == 0 and bool(np.all(k[1:] >= k[:-1]))
+    return n_sample / statistics.median(times), statistics.median(times)
+
+
+def ensure_built():
+    from cccl_gb300.build import build
+
+    build()
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all"], check=True)
+
+
+def run_reference(args):
+    rank, world = _dist()
+    if rank != 0:
+        return
+    ensure_built()
+    threads = os.cpu_count() or 1
+    n_sample = 1 << 24
+    for _ in range(args.warmup):
+        cpu_reference_sort(n_sample, threads, reps=1)
+    vals = []
+    t_total = 0.0
+    for _ in range(args.steps):
+        v, t = cpu_reference_sort(n_sample, threads, reps=1)
+        vals.append(v)
+        t_total += t
+    value = statistics.median(vals)
+    sample = f"2^24 of the 2^28 u64+u32 pairs per step (thrust::sort_by_key, OpenMP, {threads} threads)"
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1000 * t_total / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64 keys / u32 values",
+        "data": "synthetic (seeded uniform 64-bit keys)",
+        "config": {"workload": "SortPairs 2^28 u64 keys + u32 values, asc, bits 0..64 (CPU sample 2^24)",
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "reference", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_engine(args):
+    import torch
+
+    rank, world = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+        def barrier():
+            dist.barrier()
+    else:
+        def barrier():
+            pass
+    if rank == 0:
+        ensure_built()
+    if world > 1:
+        barrier()
+    from cccl_gb300.build import build
+
+    build()  # no-op when up to date
+
+    n = 1 << N_LOG2
+    keys = make_inputs(torch, n, "u64", seed=1 + rank)
+    main = Sorter(torch, keys, with_values=True)
+
+    with ClockSampler(local) as clocks:
+        ms = time_steps(torch, main.run, args.steps, args.warmup, barrier)
+    ms_t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = world * n / (ms / 1000.0)
+
+    # per-kernel durations (observer run, separate from the timed steps)
+    ktimes, launches = kernel_times(torch, main, max(3, args.steps // 2))
+    peak, peak_kind = _peaks()
+    pass_bytes = n * 2 * (8 + 4)
+    onesweep_ms = ktimes.get("onesweep")
+    achieved = pass_bytes / (onesweep_ms / 1000.0) / 1e9 if onesweep_ms else None
+    traffic = None
+    tf = ROOT / "profiles" / "onesweep_traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get("pairs_u64_u32_bytes_per_launch_at_2p28")
+
+    # end to end: pinned host buffers -> device -> sort -> host, through the same C ABI
+    hk = torch.empty(n, dtype=torch.int64, pin_memory=True)
+    hv = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    hk.copy_(keys.view(torch.int64))
+    hv.copy_(main.vi)
+    ok = torch.empty_like(hk, pin_memory=True)
+    ov = torch.empty_like(hv, pin_memory=True)
+
+    def e2e_step():
+        main.ki.view(torch.int64).copy_(hk, non_blocking=True)
+        main.vi.copy_(hv, non_blocking=True)
+        main.run()
+        ok.copy_(main.ko.view(torch.int64), non_blocking=True)
+        ov.copy_(main.vo, non_blocking=True)
+
+    e2e_steps = max(3, args.steps // 2)
+    e2e_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
+    torch.cuda.synchronize()
+
+    # variants of the configuration and the keys-only roofline row
+    variants = []
+    if not args.no_variants:
+        specs = [
+            ("entropy 51.9 bit (AND of 2)", dict(ands=2)),
+            ("entropy 34.8 bit (AND of 3)", dict(ands=3)),
+            ("entropy 12.9 bit (AND of 5)", dict(ands=5)),
+            ("constant key", dict(constant=True)),
+            ("descending", dict(descending=True)),
+            ("bits 8..40", dict(begin_bit=8, end_bit=40)),
+            ("u32 keys-only 2^28", dict(u32=True)),
+        ]
+        del main
+        torch.cuda.empty_cache()
+        for name, sp in specs:
+            if sp.get("u32"):
+                kk = make_inputs(torch, n, "u32", seed=5)
+                s = Sorter(torch, kk, with_values=False)
+            else:
+                kk = make_inputs(torch, n, "u64", ands=sp.get("ands", 1), constant=sp.get("constant", False), seed=3)
+                s = Sorter(torch, kk, with_values=True, descending=sp.get("descending", False),
+                           begin_bit=sp.get("begin_bit", 0), end_bit=sp.get("end_bit"))
+            vms = time_steps(torch, s.run, max(3, args.steps // 2), 2, barrier)
+            kt, _ = kernel_times(torch, s, 3)
+            variants.append({
+                "name": name,
+                "keys_per_s": n / (vms / 1000.0),
+                "ms": vms,
+                "passes": s.passes,
+                "roofline_frac": s.algorithmic_bytes() / (vms / 1000.0) / 1e9 / peak,
+                "onesweep_ms": kt.get("onesweep"),
+                "histogram_ms": kt.get("histogram"),
+            })
+            del s, kk
+            torch.cuda.empty_cache()
+
+    if rank != 0:
+        return
+    # CPU baseline: the reference's thrust OpenMP sort on a bounded sample (rank 0, N=1)
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cv, _ = cpu_reference_sort(1 << 24, threads, reps=3)
+        cpu = {"value": cv, "unit": UNIT, "cores": threads, "kind": "reference",
+               "sample": f"2^24 u64+u32 pairs, thrust::sort_by_key on the OpenMP backend (toolkit CCCL), {threads} threads"}
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u64 keys / u32 values (integer bit order)",
+        "data": "synthetic (seeded uniform 64-bit keys, value = index)",
+        "config": {"workload": "SortPairs 2^28 u64 keys + u32 values, asc, bits 0..64",
+                   "num_items": n, "passes": 8, "parallelism": f"replicas x{world}",
+                   "l2": "inputs (3.2 GB) larger than L2; no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "onesweep", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": pass_bytes, "launch_ms": onesweep_ms},
+        "whole_sort_roofline_frac": main_bytes(n) / (ms / 1000.0) / 1e9 / peak,
+        "kernel_ms": ktimes,
+        "gpu_launches": launches * args.steps,
+        "clocks": clocks.summary(),
+        "e2e": {"value": n / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 12,
+                "ms_per_step": e2e_ms},
+        "cpu_baseline": cpu,
+        "variants": variants,
+    }
+    print(json.dumps(line))
+
+
+def main_bytes(n):
+    return 8 * n * 2 * 12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

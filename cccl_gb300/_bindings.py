@@ -163,7 +163,10 @@ EXPORTED_SYMBOLS = [
     "cccl_device_segmented_sort_serialize",
     "cccl_device_segmented_sort_deserialize",
     "cccl_device_segmented_sort_cleanup",
+    "cccl_gb300_set_launch_observer",
 ]
+
+LAUNCH_OBSERVER = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p, C.c_int, C.c_void_p)
 
 _lib = None
 
@@ -224,8 +227,10 @@ def _declare(lib):
     lib.cccl_device_segmented_sort_cleanup.argtypes = [S]
     lib.cccl_serialization_buffer_free.argtypes = [C.c_void_p]
     lib.cccl_serialization_buffer_free.restype = None
+    lib.cccl_gb300_set_launch_observer.argtypes = [LAUNCH_OBSERVER, C.c_void_p]
+    lib.cccl_gb300_set_launch_observer.restype = None
     for name in EXPORTED_SYMBOLS:
-        if name != "cccl_serialization_buffer_free":
+        if name not in ("cccl_serialization_buffer_free", "cccl_gb300_set_launch_observer"):
             getattr(lib, name).restype = C.c_int
 
 

@@ -62,7 +62,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     sources = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(
         CSRC.glob("*.cpp")
-    ) + list((INCLUDE / "cccl" / "c").glob("*.h")) + [Path(__file__)]
+    ) + list(INCLUDE.glob("*/*.h")) + list(INCLUDE.glob("*/*/*.h")) + [Path(__file__)]
     stamp = BUILD / "stamp.txt"
     digest = _digest(sources)
     lib = library_path()

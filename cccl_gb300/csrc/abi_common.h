@@ -184,8 +184,13 @@ inline CUfunction function_of(CUkernel k)
   return f;
 }
 
+// Optional launch observer (include/cccl_gb300/sort_trace.h).
+using launch_observer_fn = void (*)(void*, const char*, int, CUstream);
+void notify_launch(const char* role, int phase, CUstream stream);
+
 template <class Params>
-inline void launch(CUkernel kernel, unsigned grid, unsigned block, size_t smem, CUstream stream, const Params& p)
+inline void launch(
+  const char* role, CUkernel kernel, unsigned grid, unsigned block, size_t smem, CUstream stream, const Params& p)
 {
   CUfunction f = function_of(kernel);
   if (smem > 48 * 1024)
@@ -194,7 +199,9 @@ inline void launch(CUkernel kernel, unsigned grid, unsigned block, size_t smem, 
           "cuFuncSetAttribute(max dynamic shared memory)");
   }
   void* args[] = {const_cast<Params*>(&p)};
+  notify_launch(role, 0, stream);
   check(cuLaunchKernel(f, grid, 1, 1, block, 1, 1, unsigned(smem), stream, args, nullptr), "cuLaunchKernel");
+  notify_launch(role, 1, stream);
 }
 
 inline int sm_count()

@@ -1,5 +1,9 @@
 // Accessors for the sm_103a cubins linked into the library. The bytes are placed by
 // the build step (cccl_gb300/build.py writes an .incbin stub next to this file's object).
+#include <atomic>
+
+#include <cccl_gb300/sort_trace.h>
+
 #include "abi_common.h"
 
 extern "C" {
@@ -36,3 +40,23 @@ image_ref segmented_image()
 }
 
 } // namespace gb300
+
+namespace
+{
+std::atomic<gb300::launch_observer_fn> g_observer{nullptr};
+std::atomic<void*> g_observer_user{nullptr};
+} // namespace
+
+void gb300::notify_launch(const char* role, int phase, CUstream stream)
+{
+  if (auto fn = g_observer.load(std::memory_order_acquire))
+  {
+    fn(g_observer_user.load(std::memory_order_relaxed), role, phase, stream);
+  }
+}
+
+extern "C" CCCL_GB300_API void cccl_gb300_set_launch_observer(cccl_gb300_launch_observer_t observer, void* user)
+{
+  g_observer_user.store(user, std::memory_order_relaxed);
+  g_observer.store(observer, std::memory_order_release);
+}

@@ -284,6 +284,7 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
   if (tid == 0)
   {
     misc[0] = atomicAdd(p.tile_counter, 1u);
+    misc[1] = 0u; // set when the look-back gave up: the tile then stores nothing
   }
   for (int i = tid; i < NW * R; i += TPB)
   {
@@ -391,6 +392,7 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
       if (failed)
       {
         atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
+        misc[1] = 1u;
       }
     }
     if (p.lookback_next != nullptr)
@@ -443,6 +445,10 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
   __syncthreads();
 
   // ---- write keys: consecutive staging slots of one digit go to consecutive outputs ----
+  // Every store is bounds-checked against the output size, so even corrupted offsets
+  // (a look-back that gave up) cannot write outside the caller's buffers.
+  const bool skip_tile               = misc[1] != 0u;
+  const unsigned long long out_limit = skip_tile ? 0ull : p.num_items_total;
   U* kout = static_cast<U*>(p.keys_out);
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j)
@@ -453,7 +459,10 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
       const U k          = kstage[s];
       const uint32_t d   = extract_digit<U, FP>(k, bit, dmask);
       const long long g  = gdelta[d] + (long long) s;
-      __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+      if ((unsigned long long) g < out_limit)
+      {
+        __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+      }
     }
   }
 
@@ -474,7 +483,10 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
       {
         const uint32_t d  = extract_digit<U, FP>(kstage[s], bit, dmask);
         const long long g = gdelta[d] + (long long) s;
-        __stcs(vout + g, vstage[s]);
+        if ((unsigned long long) g < out_limit)
+        {
+          __stcs(vout + g, vstage[s]);
+        }
       }
     }
   }

@@ -152,7 +152,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.begin_bit  = c.begin_bit;
     p.end_bit    = c.end_bit;
     p.codec      = codec;
-    launch(ks.single_tile, 1, unsigned(pol.single_tile_tpb), pol.single_tile_smem, c.stream, p);
+    launch("single_tile", ks.single_tile, 1, unsigned(pol.single_tile_tpb), pol.single_tile_smem, c.stream, p);
     *selector = 1;
     return;
   }
@@ -186,7 +186,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.words     = reinterpret_cast<uint32_t*>(ctrl);
     p.num_words = t.ctrl_bytes / 4;
     const unsigned grid = unsigned(std::min<uint64_t>(ceil_div(p.num_words, 256), 1024));
-    launch(ks.init, grid, 256, 0, c.stream, p);
+    launch("init", ks.init, grid, 256, 0, c.stream, p);
   }
   // 2. all-pass histogram + exclusive scan (+ clears pass 0's look-back)
   {
@@ -204,7 +204,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.lookback_words = t.lookback_words;
     const uint64_t want = ceil_div(n, uint64_t(pol.histogram_tpb) * (16 / kb) * 4);
     const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sm_count()) * 4)));
-    launch(ks.histogram, grid, unsigned(pol.histogram_tpb), 0, c.stream, p);
+    launch("histogram", ks.histogram, grid, unsigned(pol.histogram_tpb), 0, c.stream, p);
   }
   // 3. one onesweep launch per (pass, portion)
   void* kdst[MAX_PASSES];
@@ -243,6 +243,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.values_in     = has_vals ? static_cast<const unsigned char*>(vsrc[p]) + first * vb : nullptr;
       op.values_out    = has_vals ? vdst[p] : nullptr;
       op.portion_begin = first;
+      op.num_items_total = n;
       op.portion_items = uint32_t(items);
       op.portion_tiles = uint32_t(ceil_div(items, t.tile_items));
       op.tile_row_base = uint32_t(q * tiles_per_portion);
@@ -257,7 +258,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.num_bits      = std::min(RADIX_BITS, c.end_bit - bit);
       op.encode_in     = p == 0;
       op.decode_out    = p == passes - 1;
-      launch(ks.onesweep, op.portion_tiles, unsigned(pol.onesweep_tpb), pol.onesweep_smem, c.stream, op);
+      launch("onesweep", ks.onesweep, op.portion_tiles, unsigned(pol.onesweep_tpb), pol.onesweep_smem, c.stream, op);
     }
   }
   *selector = passes & 1;

@@ -65,6 +65,7 @@ struct OnesweepParams
   const void* values_in;      // portion-relative
   void* values_out;           // absolute
   unsigned long long portion_begin;
+  unsigned long long num_items_total; // bound of every output index
   uint32_t portion_items;
   uint32_t portion_tiles;
   uint32_t tile_row_base;     // first look-back row of this portion

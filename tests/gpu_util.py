@@ -1,0 +1,91 @@
+"""Helpers of the GPU tests: numpy <-> torch CUDA tensors and one sort through the C ABI."""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from cccl_gb300 import DoubleBuffer, SortOrder, make_radix_sort
+
+_TORCH = {
+    np.dtype(np.int8): torch.int8,
+    np.dtype(np.int16): torch.int16,
+    np.dtype(np.int32): torch.int32,
+    np.dtype(np.int64): torch.int64,
+    np.dtype(np.uint8): torch.uint8,
+    np.dtype(np.float16): torch.float16,
+    np.dtype(np.float32): torch.float32,
+    np.dtype(np.float64): torch.float64,
+    np.dtype(np.bool_): torch.bool,
+}
+for _n in ("uint16", "uint32", "uint64"):
+    if hasattr(torch, _n):
+        _TORCH[np.dtype(_n)] = getattr(torch, _n)
+
+
+def to_dev(a: np.ndarray) -> torch.Tensor:
+    """Bit-exact copy of a numpy array to the GPU (torch dtypes it lacks go as raw bytes)."""
+    a = np.ascontiguousarray(a)
+    td = _TORCH.get(a.dtype)
+    if td is None:
+        raise TypeError(a.dtype)
+    t = torch.empty(a.size, dtype=td, device="cuda")
+    t.view(torch.uint8).copy_(torch.from_numpy(a.view(np.uint8).reshape(-1)))
+    return t
+
+
+def from_dev(t: torch.Tensor, dtype) -> np.ndarray:
+    raw = t.view(torch.uint8).cpu().numpy()
+    return raw.view(np.dtype(dtype))
+
+
+def empty_like_dev(a: np.ndarray) -> torch.Tensor:
+    return torch.empty(a.size, dtype=_TORCH[np.dtype(a.dtype)], device="cuda")
+
+
+def value_tensor(v: np.ndarray) -> torch.Tensor:
+    """Values of any width, carried as raw words of their size."""
+    words = {1: torch.uint8, 2: torch.int16, 4: torch.int32, 8: torch.int64}
+    if v.dtype.itemsize in words:
+        t = torch.empty(v.size, dtype=words[v.dtype.itemsize], device="cuda")
+        t.view(torch.uint8).copy_(torch.from_numpy(np.ascontiguousarray(v).view(np.uint8).reshape(-1)))
+        return t
+    # 16-byte values: complex128 has the width and alignment
+    assert v.dtype.itemsize == 16
+    t = torch.empty(v.size, dtype=torch.complex128, device="cuda")
+    t.view(torch.uint8).copy_(torch.from_numpy(np.ascontiguousarray(v).view(np.uint8).reshape(-1)))
+    return t
+
+
+def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, overwrite=False, return_temp=False):
+    """Sorts through cccl_device_radix_sort. Returns (keys, values, selector[, temp])."""
+    order = SortOrder.DESCENDING if descending else SortOrder.ASCENDING
+    ki = to_dev(keys)
+    ko = empty_like_dev(keys)
+    vi = vo = None
+    if values is not None:
+        vi = value_tensor(values)
+        vo = torch.empty_like(vi)
+    if overwrite:
+        dk = DoubleBuffer(ki, ko)
+        dv = DoubleBuffer(vi, vo) if vi is not None else None
+        args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
+    else:
+        args = dict(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo)
+    sorter = make_radix_sort(order=order, **args)
+    nbytes = sorter(temp_storage=None, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit, **args)
+    temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
+    sorter(temp_storage=temp, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit, **args)
+    torch.cuda.synchronize()
+    if overwrite:
+        sel = dk.selector
+        kout = dk.current()
+        vout = dv.current() if dv is not None else None
+    else:
+        sel = None
+        kout, vout = ko, vo
+    kres = from_dev(kout, keys.dtype)
+    vres = from_dev(vout, values.dtype) if values is not None else None
+    if return_temp:
+        return kres, vres, sel, temp
+    return kres, vres, sel

@@ -20,9 +20,10 @@ def lib(built_library):
 
 def header_symbols():
     names = set()
-    for h in (ROOT / "include" / "cccl" / "c").glob("*.h"):
-        names |= set(re.findall(r"CCCL_C_API\s+(?:\w+\s+)*?(cccl_\w+)\s*\(", h.read_text()))
-        names |= set(re.findall(r"CCCL_C_API\s+CUresult\s*\n\s*(cccl_\w+)\s*\(", h.read_text()))
+    for h in (ROOT / "include").glob("**/*.h"):
+        text = h.read_text()
+        names |= set(re.findall(r"CCCL_(?:C|GB300)_API\s+(?:\w+\s+)*?(cccl_\w+)\s*\(", text))
+        names |= set(re.findall(r"CCCL_C_API\s+CUresult\s*\n\s*(cccl_\w+)\s*\(", text))
     return names
 
 

@@ -1,0 +1,205 @@
+"""Parity of the GPU radix sort (through the C ABI) with the oracle and the reference's
+golden vectors, plus the reference's edge cases (cub/test/catch2_test_device_radix_sort_keys.cu,
+..._pairs.cu, c/parallel/test/test_radix_sort.cpp). Bit-exact everywhere."""
+
+import glob
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import inputs as I
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(str(Path(__file__).parent / "golden" / "radix_*.npz")))
+SINGLE_TILE_4B = 4864  # CUB's single-tile cut for 4-byte keys
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_library):
+    import torch
+
+    assert torch.cuda.is_available()
+    return built_library
+
+
+def _check(oracle, keys, values=None, b=0, e=None, desc=False, overwrite=False):
+    from gpu_util import gpu_sort
+
+    ko, vo, sel = gpu_sort(keys, values, b, e, desc, overwrite)
+    rk, rv = oracle.radix_sort(keys, values, b, e, desc, threads=4)
+    assert ko.tobytes() == rk.tobytes(), "keys differ from the oracle"
+    if values is not None:
+        assert vo.tobytes() == rv.tobytes(), "values differ from the oracle"
+    return sel
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: Path(p).stem)
+def test_golden_vectors(path):
+    from gpu_util import gpu_sort
+
+    g = np.load(path)
+    vals = g["values_in"] if "values_in" in g else None
+    ko, vo, _ = gpu_sort(g["keys_in"], vals, int(g["begin_bit"]), int(g["end_bit"]), bool(g["descending"]))
+    assert ko.tobytes() == g["keys_out"].tobytes()
+    if vals is not None:
+        assert vo.tobytes() == g["values_out"].tobytes()
+
+
+KEY_TYPES = [np.uint8, np.int8, np.uint16, np.int16, np.float16, np.uint32, np.int32, np.float32, np.uint64,
+             np.int64, np.float64]
+
+
+@pytest.mark.parametrize("n", [1, 17, SINGLE_TILE_4B, SINGLE_TILE_4B + 1, 300_001])
+@pytest.mark.parametrize("dtype", KEY_TYPES, ids=lambda d: np.dtype(d).name)
+def test_keys_and_pairs_vs_oracle(oracle, dtype, n):
+    rng = np.random.default_rng(n * 31 + np.dtype(dtype).itemsize)
+    if np.dtype(dtype).kind == "f":
+        k = I.with_specials(I.finite_floats(dtype, n, rng), rng, 1 / 16)
+    else:
+        k = I.uniform_bits(dtype, n, rng)
+    for desc in (False, True):
+        _check(oracle, k, None, desc=desc)
+        _check(oracle, k, I.index_values(n), desc=desc)
+
+
+@pytest.mark.parametrize("vbytes", [1, 2, 4, 8, 16])
+def test_value_widths(oracle, vbytes):
+    rng = np.random.default_rng(vbytes)
+    n = 200_003
+    k = I.entropy_reduced(np.uint32, n, rng, 3)
+    v = rng.integers(0, 255, size=n * vbytes, dtype=np.uint8).view(f"V{vbytes}") if vbytes == 16 else \
+        I.uniform_bits({1: np.uint8, 2: np.uint16, 4: np.uint32, 8: np.uint64}[vbytes], n, rng)
+    if vbytes == 16:
+        from gpu_util import gpu_sort
+
+        ko, vo, _ = gpu_sort(k, v.view(np.uint8).reshape(n, 16).view(np.complex128).reshape(n))
+        perm = oracle.radix_permutation(k)
+        assert ko.tobytes() == k[perm].tobytes()
+        assert vo.tobytes() == v[perm].tobytes()
+    else:
+        _check(oracle, k, v)
+
+
+@pytest.mark.parametrize(
+    "dtype,b,e", [(np.uint32, 0, 5), (np.uint32, 3, 27), (np.int32, 16, 32), (np.float32, 0, 31), (np.uint64, 8, 40),
+                  (np.float64, 1, 63), (np.uint16, 4, 13), (np.uint64, 60, 64)]
+)
+def test_bit_windows(oracle, dtype, b, e):
+    rng = np.random.default_rng(b * 100 + e)
+    n = 123_457
+    k = I.uniform_bits(dtype, n, rng)
+    for desc in (False, True):
+        _check(oracle, k, I.index_values(n), b, e, desc)
+
+
+@pytest.mark.parametrize("ands", [1, 3, 9, 15])
+def test_entropy_reduction(oracle, ands):
+    rng = np.random.default_rng(ands)
+    k = I.entropy_reduced(np.uint64, 500_000, rng, ands)
+    _check(oracle, k, I.index_values(k.size))
+    _check(oracle, k, I.index_values(k.size), desc=True)
+
+
+def test_negative_zero_bitwise(oracle):
+    rng = np.random.default_rng(11)
+    for dtype in (np.float32, np.float64, np.float16):
+        k = I.finite_floats(dtype, 100_000, rng)
+        k[rng.choice(k.size, k.size // 128, replace=False)] = dtype(-0.0)
+        k[rng.choice(k.size, k.size // 128, replace=False)] = dtype(0.0)
+        for desc in (False, True):
+            _check(oracle, k, I.index_values(k.size), desc=desc)
+
+
+def test_uniform_values(oracle):
+    for dtype in (np.uint32, np.float64, np.int8):
+        k = np.full(100_000, 5, dtype=dtype)
+        _check(oracle, k, I.index_values(k.size))
+        _check(oracle, k, I.index_values(k.size), desc=True)
+
+
+@pytest.mark.parametrize("n", [100, SINGLE_TILE_4B + 1, 1_000_000])
+@pytest.mark.parametrize("bits", [(0, 32), (0, 8), (0, 16), (4, 28)])
+def test_double_buffer_selector(oracle, n, bits):
+    """With is_overwrite_okay the result is wherever the selector points; the selector
+    equals CUB's: 1 for the single-tile path, passes & 1 otherwise."""
+    rng = np.random.default_rng(n)
+    k = I.uniform_bits(np.uint32, n, rng)
+    sel = _check(oracle, k, I.index_values(n), bits[0], bits[1], overwrite=True)
+    passes = -(-(bits[1] - bits[0]) // 8)
+    expect = 1 if n <= SINGLE_TILE_4B else passes & 1
+    assert sel == expect
+
+
+def test_begin_equals_end(oracle):
+    from gpu_util import gpu_sort
+
+    k = I.uniform_bits(np.uint32, 10_000, np.random.default_rng(0))
+    ko, _, _ = gpu_sort(k, None, 7, 7)  # copy
+    assert ko.tobytes() == k.tobytes()
+    ko, _, sel = gpu_sort(k, None, 7, 7, overwrite=True)  # nothing to do, data stays put
+    assert sel == 0 and ko.tobytes() == k.tobytes()
+
+
+def test_empty_input():
+    import torch
+
+    from cccl_gb300 import SortOrder, make_radix_sort
+
+    k = torch.empty(0, dtype=torch.int32, device="cuda")
+    s = make_radix_sort(d_in_keys=k, d_out_keys=k, d_in_values=None, d_out_values=None, order=SortOrder.ASCENDING)
+    assert s(temp_storage=None, d_in_keys=k, d_out_keys=k, d_in_values=None, d_out_values=None, num_items=0) == 1
+
+
+def test_c_abi_reference_cases(oracle):
+    """c/parallel/test/test_radix_sort.cpp:180-330: uint8/int16/uint32/half/double keys,
+    float items, descending and overwrite variants, 500 / 1e6 / 2e6 / random sizes."""
+    rng = np.random.default_rng(2024)
+    params = [(np.uint8, False, False), (np.int16, True, False), (np.uint32, False, True), (np.float16, True, True),
+              (np.float64, False, False)]
+    for dtype, desc, ow in params:
+        for n in (500, 1_000_000, 2_000_000, int(rng.integers(1, 1_000_000))):
+            if np.dtype(dtype).kind == "f":
+                k = rng.permutation(n).astype(dtype)
+            else:
+                k = (rng.permutation(n) % (np.iinfo(dtype).max + 1)).astype(dtype)
+            items = k.astype(np.float32)
+            _check(oracle, k, items, desc=desc, overwrite=ow)
+
+
+def test_status_word_clean_after_sort():
+    import torch
+
+    from gpu_util import gpu_sort
+
+    k = I.uniform_bits(np.uint32, 3_000_000, np.random.default_rng(5))
+    _, _, _, temp = gpu_sort(k, None, return_temp=True)
+    status = temp[: 16 * 1024 + 8].view(torch.int32)[4097].item()  # SortControl::status
+    assert status == 0
+
+
+def test_large_full_size_properties():
+    """2^28 keys (the benchmark size): sorted, stable and a permutation, checked on the
+    GPU with independent torch operations."""
+    import torch
+
+    from cccl_gb300 import SortOrder, make_radix_sort
+
+    n = 1 << 28
+    g = torch.Generator(device="cuda").manual_seed(3)
+    k = torch.randint(0, 1 << 20, (n,), device="cuda", dtype=torch.int32, generator=g)
+    v = torch.arange(n, device="cuda", dtype=torch.int32)
+    ko, vo = torch.empty_like(k), torch.empty_like(v)
+    s = make_radix_sort(d_in_keys=k, d_out_keys=ko, d_in_values=v, d_out_values=vo, order=SortOrder.ASCENDING)
+    nb = s(temp_storage=None, d_in_keys=k, d_out_keys=ko, d_in_values=v, d_out_values=vo, num_items=n)
+    t = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    s(temp_storage=t, d_in_keys=k, d_out_keys=ko, d_in_values=v, d_out_values=vo, num_items=n)
+    torch.cuda.synchronize()
+    assert bool((ko[1:] >= ko[:-1]).all())
+    eq = ko[1:] == ko[:-1]
+    assert bool((vo[1:][eq] > vo[:-1][eq]).all())  # stable: equal keys keep index order
+    assert bool((k[vo.long()] == ko).all())  # values are the source positions of the keys
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    cnt.index_add_(0, vo.long(), torch.ones_like(vo))
+    assert bool((cnt == 1).all())
