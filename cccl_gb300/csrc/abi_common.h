@@ -204,6 +204,43 @@ inline void launch(
   notify_launch(role, 1, stream);
 }
 
+// Cooperative launch: every CTA of the grid is resident at once (the persistent kernels
+// wait on each other's tiles, so co-residency is required for forward progress).
+template <class Params>
+inline void launch_cooperative(
+  const char* role, CUkernel kernel, unsigned grid, unsigned block, size_t smem, CUstream stream, const Params& p)
+{
+  CUfunction f = function_of(kernel);
+  if (smem > 48 * 1024)
+  {
+    check(cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, int(smem)),
+          "cuFuncSetAttribute(max dynamic shared memory)");
+  }
+  void* args[] = {const_cast<Params*>(&p)};
+  notify_launch(role, 0, stream);
+  check(cuLaunchCooperativeKernel(f, grid, 1, 1, block, 1, 1, unsigned(smem), stream, args),
+        "cuLaunchCooperativeKernel");
+  notify_launch(role, 1, stream);
+}
+
+// Resident CTAs per SM of a kernel at the given block size and dynamic shared memory.
+inline int occupancy(CUkernel kernel, int block, size_t smem)
+{
+  CUfunction f = function_of(kernel);
+  if (smem > 48 * 1024)
+  {
+    check(cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, int(smem)),
+          "cuFuncSetAttribute(max dynamic shared memory)");
+  }
+  int n = 0;
+  check(cuOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, block, smem), "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+  if (n < 1)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "kernel cannot be resident on an SM");
+  }
+  return n;
+}
+
 inline int sm_count()
 {
   CUdevice dev;

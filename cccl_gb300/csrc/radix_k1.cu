@@ -2,4 +2,5 @@
 #include "radix_instances.cuh"
 
 GB300_ALL_VALUES(1, false, i)
+GB300_ONESWEEP_FIRST(1)
 

@@ -2,4 +2,5 @@
 #include "radix_instances.cuh"
 
 GB300_ALL_VALUES(2, false, i)
+GB300_ONESWEEP_FIRST(2)
 GB300_ALL_VALUES(2, true, f)

@@ -23,71 +23,10 @@
 //    so no memset runs between passes.
 #pragma once
 
-#include "sort_common.cuh"
+#include "tile_rank.cuh"
 
 namespace gb300
 {
-
-__device__ __forceinline__ void named_barrier_256()
-{
-  asm volatile("bar.sync 1, 256;" ::: "memory");
-}
-
-// Exclusive prefix over the 256 digit slots held by threads [0, 256) (one value per
-// thread). `scratch` holds 8 words. Must be called by exactly threads [0, 256).
-__device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch)
-{
-  const int tid  = threadIdx.x;
-  const int lane = tid & 31;
-  const int w    = tid >> 5;
-  uint32_t x     = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1)
-  {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o)
-    {
-      x += y;
-    }
-  }
-  if (lane == 31)
-  {
-    scratch[w] = x;
-  }
-  named_barrier_256();
-  uint32_t pre = 0;
-#pragma unroll
-  for (int j = 0; j < 8; ++j)
-  {
-    pre += (j < w) ? scratch[j] : 0u;
-  }
-  return pre + x - v;
-}
-
-// Stable rank of one warp's keys: in round i lane l holds the key at warp-local index
-// i*32+l, so (round, lane) order is source order. rank[i] = number of earlier keys of
-// the warp with the same digit. Per-warp digit counters live in whist_w[RADIX_DIGITS].
-template <class U, bool FP, int ITEMS>
-__device__ __forceinline__ void warp_rank(
-  const U (&keys)[ITEMS], uint32_t (&rank)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
-{
-  const uint32_t lt = lanemask_lt();
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i)
-  {
-    const uint32_t d     = extract_digit<U, FP>(keys[i], bit, dmask);
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t below = __popc(peers & lt);
-    const uint32_t base  = whist_w[d];
-    rank[i]              = base + below;
-    __syncwarp();
-    if (below == 0)
-    {
-      whist_w[d] = base + __popc(peers);
-    }
-    __syncwarp();
-  }
-}
 
 // ---------------------------------------------------------------------------------------
 // init: zero a block of 32-bit words (the per-call control block)
@@ -242,257 +181,6 @@ __device__ __forceinline__ void histogram_body(const HistogramParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
-// onesweep: one stable digit pass over one portion
-// ---------------------------------------------------------------------------------------
-template <int KB, int VB, int TPB, int ITEMS>
-struct OnesweepSmem
-{
-  using U              = typename uint_of<KB>::type;
-  using V              = typename value_word<VB>::type;
-  static constexpr int NW   = TPB / 32;
-  static constexpr int TILE = TPB * ITEMS;
-  static constexpr size_t whist_off  = 0;
-  static constexpr size_t gdelta_off = whist_off + sizeof(uint32_t) * NW * RADIX_DIGITS;
-  static constexpr size_t misc_off   = gdelta_off + sizeof(long long) * RADIX_DIGITS;
-  static constexpr size_t kstage_off = misc_off + 128;
-  static constexpr size_t vstage_off = kstage_off + ((sizeof(U) * TILE + 15) / 16) * 16;
-  static constexpr size_t bytes      = vstage_off + (VB > 0 ? sizeof(V) * TILE : 0);
-};
-
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
-__device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
-{
-  using L              = OnesweepSmem<KB, VB, TPB, ITEMS>;
-  using U              = typename L::U;
-  using V              = typename L::V;
-  constexpr int NW     = L::NW;
-  constexpr int TILE   = L::TILE;
-  constexpr int R      = RADIX_DIGITS;
-  static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
-
-  extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
-  long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
-  uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);
-  U* kstage         = reinterpret_cast<U*>(smem + L::kstage_off);
-  V* vstage         = reinterpret_cast<V*>(smem + L::vstage_off);
-
-  const int tid  = threadIdx.x;
-  const int lane = tid & 31;
-  const int warp = tid >> 5;
-
-  if (tid == 0)
-  {
-    misc[0] = atomicAdd(p.tile_counter, 1u);
-    misc[1] = 0u; // set when the look-back gave up: the tile then stores nothing
-  }
-  for (int i = tid; i < NW * R; i += TPB)
-  {
-    whist[i] = 0;
-  }
-  __syncthreads();
-
-  const uint32_t tile       = misc[0];
-  const uint32_t tile_first = tile * TILE;
-  const uint32_t valid      = min(uint32_t(TILE), p.portion_items - tile_first);
-  const bool full           = valid == uint32_t(TILE);
-  const int bit             = p.current_bit;
-  const uint32_t dmask      = (1u << p.num_bits) - 1u;
-
-  // ---- load (warp-striped, coalesced) ----
-  const U* kin   = static_cast<const U*>(p.keys_in) + tile_first;
-  const int wofs = warp * ITEMS * 32 + lane;
-  U keys[ITEMS];
-  if (full)
-  {
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
-    {
-      keys[i] = __ldcs(kin + wofs + i * 32);
-    }
-    if (p.encode_in)
-    {
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i)
-      {
-        keys[i] = encode_key<U>(keys[i], p.codec);
-      }
-    }
-  }
-  else
-  {
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
-    {
-      const uint32_t idx = wofs + i * 32;
-      U k                = U(~U(0));
-      if (idx < valid)
-      {
-        k = kin[idx];
-        if (p.encode_in)
-        {
-          k = encode_key<U>(k, p.codec);
-        }
-      }
-      keys[i] = k;
-    }
-  }
-
-  // ---- stable in-tile rank ----
-  uint32_t rank[ITEMS];
-  warp_rank<U, FP, ITEMS>(keys, rank, whist + warp * R, bit, dmask);
-  __syncthreads();
-
-  // ---- per-digit totals, publish, tile-local digit starts ----
-  uint32_t total = 0;
-  uint32_t tstart = 0;
-  uint32_t* lb_row = p.lookback + (size_t) (p.tile_row_base + tile) * R;
-  if (tid < R)
-  {
-#pragma unroll
-    for (int w = 0; w < NW; ++w)
-    {
-      const uint32_t c  = whist[w * R + tid];
-      whist[w * R + tid] = total;
-      total += c;
-    }
-    store_status(lb_row + tid, (tile == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
-    tstart = digit_exclusive_scan(total, misc + 8);
-#pragma unroll
-    for (int w = 0; w < NW; ++w)
-    {
-      whist[w * R + tid] += tstart;
-    }
-  }
-  __syncthreads();
-
-  // ---- decoupled look-back (threads [0, 256), one digit each) ----
-  if (tid < R)
-  {
-    uint32_t excl = 0;
-    bool failed   = false;
-    if (tile > 0)
-    {
-      for (int j = int(tile) - 1; j >= 0; --j)
-      {
-        const uint32_t v = wait_status(p.lookback + (size_t) (p.tile_row_base + j) * R + tid);
-        const uint32_t f = v & LB_FLAGS;
-        if (f == LB_ERROR)
-        {
-          failed = true;
-          break;
-        }
-        excl += v & LB_VALUE;
-        if (f == LB_INCLUSIVE)
-        {
-          break;
-        }
-      }
-      store_status(lb_row + tid, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
-      if (failed)
-      {
-        atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
-        misc[1] = 1u;
-      }
-    }
-    if (p.lookback_next != nullptr)
-    {
-      p.lookback_next[(size_t) (p.tile_row_base + tile) * R + tid] = 0u;
-    }
-    const unsigned long long base = p.bins[tid] + excl;
-    gdelta[tid]                   = (long long) base - (long long) tstart;
-    if (p.bins_next != nullptr && tile == p.portion_tiles - 1)
-    {
-      p.bins_next[tid] = base + total;
-    }
-  }
-
-  // ---- scatter keys into the digit-sorted staging tile ----
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i)
-  {
-    const uint32_t d   = extract_digit<U, FP>(keys[i], bit, dmask);
-    const uint32_t pos = whist[warp * R + d] + rank[i];
-    kstage[pos]        = keys[i];
-    rank[i]            = pos;
-  }
-
-  V vals[VB > 0 ? ITEMS : 1];
-  if constexpr (VB > 0)
-  {
-    const V* vin = static_cast<const V*>(p.values_in) + tile_first;
-    if (full)
-    {
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i)
-      {
-        vals[i] = __ldcs(vin + wofs + i * 32);
-      }
-    }
-    else
-    {
-#pragma unroll
-      for (int i = 0; i < ITEMS; ++i)
-      {
-        const uint32_t idx = wofs + i * 32;
-        if (idx < valid)
-        {
-          vals[i] = vin[idx];
-        }
-      }
-    }
-  }
-  __syncthreads();
-
-  // ---- write keys: consecutive staging slots of one digit go to consecutive outputs ----
-  // Every store is bounds-checked against the output size, so even corrupted offsets
-  // (a look-back that gave up) cannot write outside the caller's buffers.
-  const bool skip_tile               = misc[1] != 0u;
-  const unsigned long long out_limit = skip_tile ? 0ull : p.num_items_total;
-  U* kout = static_cast<U*>(p.keys_out);
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j)
-  {
-    const uint32_t s = j * TPB + tid;
-    if (full || s < valid)
-    {
-      const U k          = kstage[s];
-      const uint32_t d   = extract_digit<U, FP>(k, bit, dmask);
-      const long long g  = gdelta[d] + (long long) s;
-      if ((unsigned long long) g < out_limit)
-      {
-        __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
-      }
-    }
-  }
-
-  if constexpr (VB > 0)
-  {
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
-    {
-      vstage[rank[i]] = vals[i];
-    }
-    __syncthreads();
-    V* vout = static_cast<V*>(p.values_out);
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j)
-    {
-      const uint32_t s = j * TPB + tid;
-      if (full || s < valid)
-      {
-        const uint32_t d  = extract_digit<U, FP>(kstage[s], bit, dmask);
-        const long long g = gdelta[d] + (long long) s;
-        if ((unsigned long long) g < out_limit)
-        {
-          __stcs(vout + g, vstage[s]);
-        }
-      }
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------------------
 // single tile: the whole LSD sort of <= TPB*ITEMS keys inside one CTA
 // ---------------------------------------------------------------------------------------
 template <int KB, int TPB, int ITEMS>
@@ -560,34 +248,21 @@ __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
     {
       keys[i] = src[wofs + i * 32];
     }
-    uint32_t rank[ITEMS];
-    warp_rank<U, FP, ITEMS>(keys, rank, whist + warp * R, bit, dmask);
+    warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
     __syncthreads();
     if (tid < R)
     {
-      uint32_t total = 0;
-#pragma unroll
-      for (int w = 0; w < NW; ++w)
-      {
-        const uint32_t c  = whist[w * R + tid];
-        whist[w * R + tid] = total;
-        total += c;
-      }
-      const uint32_t tstart = digit_exclusive_scan(total, misc + 8);
-#pragma unroll
-      for (int w = 0; w < NW; ++w)
-      {
-        whist[w * R + tid] += tstart;
-      }
+      uint32_t tstart;
+      block_digit_offsets<NW>(whist, misc + 8, &tstart);
     }
     __syncthreads();
+    uint32_t pos[ITEMS];
+    warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i)
     {
-      const uint32_t d   = extract_digit<U, FP>(keys[i], bit, dmask);
-      const uint32_t pos = whist[warp * R + d] + rank[i];
-      dst[pos]           = keys[i];
-      id[pos]            = is[wofs + i * 32];
+      dst[pos[i]] = keys[i];
+      id[pos[i]]  = is[wofs + i * 32];
     }
     __syncthreads();
     cur ^= 1;
@@ -607,3 +282,5 @@ __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
 }
 
 } // namespace gb300
+
+#include "onesweep.cuh"

@@ -29,6 +29,9 @@ RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind)
   p.single_tile_items = SINGLE_TILE_ITEMS;
   p.histogram_tpb     = HISTOGRAM_TPB;
   p.onesweep_smem     = onesweep_smem_bytes(key_bytes, value_bytes);
+  p.persistent_tpb    = PERSISTENT_TPB;
+  p.persistent_items  = persistent_items(key_bytes, value_bytes);
+  p.persistent_smem   = persistent_smem_bytes(key_bytes, value_bytes);
   p.single_tile_smem  = single_tile_smem_bytes(key_bytes);
   return p;
 }
@@ -38,11 +41,13 @@ static uint64_t ceil_div(uint64_t a, uint64_t b)
   return (a + b - 1) / b;
 }
 
-RadixTempPlan plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, bool need_tmp)
+RadixTempPlan
+plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, bool need_tmp, bool persistent)
 {
   RadixTempPlan t{};
   t.num_passes    = int(ceil_div(uint64_t(end_bit - begin_bit), RADIX_BITS));
-  t.tile_items    = uint64_t(pol.onesweep_tpb) * pol.onesweep_items;
+  t.tile_items    = persistent ? uint64_t(pol.persistent_tpb) * pol.persistent_items
+                               : uint64_t(pol.onesweep_tpb) * pol.onesweep_items;
   // Look-back words carry a 30-bit count, so one launch covers < 2^30 keys.
   t.portion_items = ((1ull << 30) - 1) / t.tile_items * t.tile_items;
   t.num_portions  = ceil_div(n, t.portion_items);
@@ -69,6 +74,11 @@ RadixTempPlan plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit,
   }
   t.total_bytes = off;
   return t;
+}
+
+static bool aligned16(const void* p)
+{
+  return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
 }
 
 static void check_aligned(const void* p, size_t a, const char* what)
@@ -159,7 +169,11 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
 
   const int passes    = int(ceil_div(uint64_t(c.end_bit - c.begin_bit), RADIX_BITS));
   const bool need_tmp = !c.overwrite && passes > 1;
-  const RadixTempPlan t = plan_radix_temp(pol, n, c.begin_bit, c.end_bit, need_tmp);
+  // The persistent kernel bulk-copies tiles straight from the pass inputs, which needs
+  // 16-byte aligned buffers; otherwise every pass uses the CTA-per-tile kernel.
+  const bool persistent = aligned16(c.keys[0]) && aligned16(c.keys[1])
+                       && (!has_vals || (aligned16(c.values[0]) && aligned16(c.values[1])));
+  const RadixTempPlan t = plan_radix_temp(pol, n, c.begin_bit, c.end_bit, need_tmp, persistent);
   if (c.d_temp_storage == nullptr)
   {
     *c.temp_storage_bytes = t.total_bytes;
@@ -258,7 +272,20 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.num_bits      = std::min(RADIX_BITS, c.end_bit - bit);
       op.encode_in     = p == 0;
       op.decode_out    = p == passes - 1;
-      launch("onesweep", ks.onesweep, op.portion_tiles, unsigned(pol.onesweep_tpb), pol.onesweep_smem, c.stream, op);
+      if (persistent)
+      {
+        const bool order_free =
+          p == 0 && !has_vals && pol.key_kind != KIND_FLOAT && c.begin_bit == 0 && c.end_bit == 8 * kb;
+        const CUkernel k    = order_free ? ks.onesweep_first : ks.onesweep;
+        const unsigned grid = unsigned(std::min<uint64_t>(
+          op.portion_tiles, uint64_t(sm_count()) * occupancy(k, pol.persistent_tpb, pol.persistent_smem)));
+        launch_cooperative("onesweep", k, grid, unsigned(pol.persistent_tpb), pol.persistent_smem, c.stream, op);
+      }
+      else
+      {
+        launch("onesweep", ks.onesweep_dyn, op.portion_tiles, unsigned(pol.onesweep_tpb), pol.onesweep_smem, c.stream,
+               op);
+      }
     }
   }
   *selector = passes & 1;

@@ -25,9 +25,12 @@ struct RadixPolicy
   int32_t single_tile_tpb;
   int32_t single_tile_items;
   int32_t histogram_tpb;
-  int32_t reserved[7];
+  int32_t persistent_tpb;
+  int32_t persistent_items;
+  int32_t reserved[5];
   uint64_t onesweep_smem;
   uint64_t single_tile_smem;
+  uint64_t persistent_smem;
 };
 
 RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind);
@@ -36,7 +39,9 @@ struct RadixKernels
 {
   CUkernel init;
   CUkernel histogram;
-  CUkernel onesweep;
+  CUkernel onesweep;       // persistent pass kernel (bulk-copy prefetch, cooperative launch)
+  CUkernel onesweep_first; // its order-free variant for pass 0 of integer keys-only sorts (may be == onesweep)
+  CUkernel onesweep_dyn;   // CTA-per-tile pass kernel for buffers that are not 16-byte aligned
   CUkernel single_tile;
 };
 
@@ -69,7 +74,8 @@ struct RadixTempPlan
   size_t total_bytes;
 };
 
-RadixTempPlan plan_radix_temp(const RadixPolicy& pol, uint64_t num_items, int begin_bit, int end_bit, bool need_tmp);
+RadixTempPlan plan_radix_temp(
+  const RadixPolicy& pol, uint64_t num_items, int begin_bit, int end_bit, bool need_tmp, bool persistent);
 
 // Runs (or sizes, when d_temp_storage is null) one sort. Writes the DoubleBuffer
 // selector CUB would report. Throws cuda_error on failure.

@@ -143,6 +143,9 @@ try
   const std::string s   = suffix(kind);
   const std::string kv  = "k" + std::to_string(key_bytes) + "_v" + std::to_string(value_size) + "_" + s;
   const std::string one = "gb300_onesweep_" + kv;
+  const std::string dyn = "gb300_onesweep_dyn_" + kv;
+  // integer keys-only sorts have an order-free first-pass kernel
+  const std::string first = (value_size == 0 && kind != KIND_FLOAT) ? "gb300_onesweep_first_" + kv : one;
   const std::string st  = "gb300_single_tile_" + kv;
   const std::string his = "gb300_histogram_k" + std::to_string(key_bytes) + "_" + s;
   const std::string ini = "gb300_init";
@@ -161,8 +164,8 @@ try
   r.upsweep_kernel_lowered_name                = dup_cstr(his);
   r.alt_upsweep_kernel_lowered_name            = dup_cstr(his);
   r.scan_bins_kernel_lowered_name              = dup_cstr(his);
-  r.downsweep_kernel_lowered_name              = dup_cstr(one);
-  r.alt_downsweep_kernel_lowered_name          = dup_cstr(one);
+  r.downsweep_kernel_lowered_name              = dup_cstr(dyn);
+  r.alt_downsweep_kernel_lowered_name          = dup_cstr(first);
   r.histogram_kernel_lowered_name              = dup_cstr(his);
   r.exclusive_sum_kernel_lowered_name          = dup_cstr(his);
   r.init_bins_and_counters_kernel_lowered_name = dup_cstr(ini);
@@ -342,6 +345,8 @@ CCCL_C_API CUresult cccl_device_radix_sort(
     RadixKernels ks{build.init_bins_and_counters_kernel,
                     build.histogram_kernel,
                     build.onesweep_kernel,
+                    build.alt_downsweep_kernel,
+                    build.downsweep_kernel,
                     build.single_tile_kernel};
     RadixCall call{};
     call.keys[0]          = d_keys_in.state;

@@ -12,6 +12,7 @@ constexpr int RADIX_BITS    = 8;
 constexpr int RADIX_DIGITS  = 1 << RADIX_BITS;
 constexpr int MAX_PASSES    = 8; // 64-bit keys
 constexpr uint64_t LOOKBACK_TIMEOUT_NS = 1000000000ull; // 1 s
+constexpr int LOOKBACK_BATCH = 8; // predecessor rows read per look-back step
 
 // Status word bits reported by the kernels (OR-ed into SortControl::status).
 constexpr uint32_t STATUS_LOOKBACK_TIMEOUT = 1u;

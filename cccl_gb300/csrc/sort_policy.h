@@ -19,7 +19,8 @@
 namespace gb300
 {
 
-constexpr int ONESWEEP_TPB     = 384;
+constexpr int ONESWEEP_TPB     = 384; // CTA-per-tile fallback kernel
+constexpr int PERSISTENT_TPB   = 512; // persistent onesweep kernel (one CTA per SM)
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
 constexpr int HISTOGRAM_TPB    = 512;
@@ -51,6 +52,20 @@ GB300_HD constexpr size_t onesweep_smem_bytes(int kb, int vb)
        + (vb > 0 ? value_word_bytes(vb) * ONESWEEP_TPB * onesweep_items(kb, vb) : 0);
 }
 
+// Items per thread of the persistent onesweep kernel: the two tile buffers (keys + values)
+// must fit the 227 KB of shared memory next to the 16 KB of per-warp counters.
+GB300_HD constexpr int persistent_items(int kb, int vb)
+{
+  return vb >= 16 ? 8 : kb == 8 ? 12 : kb == 4 ? (vb == 0 ? 20 : vb <= 4 ? 16 : 12) : 16;
+}
+
+GB300_HD constexpr size_t persistent_smem_bytes(int kb, int vb)
+{
+  return size_t(4) * (PERSISTENT_TPB / 32) * 256 + size_t(8) * 256 + 128
+       + 2 * (round16(size_t(kb) * PERSISTENT_TPB * persistent_items(kb, vb))
+              + (vb > 0 ? value_word_bytes(vb) * PERSISTENT_TPB * persistent_items(kb, vb) : 0));
+}
+
 GB300_HD constexpr int single_tile_capacity()
 {
   return SINGLE_TILE_TPB * SINGLE_TILE_ITEMS;
@@ -78,5 +93,8 @@ GB300_HD constexpr unsigned long long cub_single_tile_limit(int key_bytes, int v
 static_assert(cub_single_tile_limit(4, 0) == 4864, "CUB single-tile cut, 4-byte keys");
 static_assert(cub_single_tile_limit(8, 4) == 2304, "CUB single-tile cut, 8-byte keys");
 static_assert(cub_single_tile_limit(4, 16) == 1024, "CUB single-tile cut, 16-byte values");
+static_assert(persistent_smem_bytes(8, 8) <= 227 * 1024 && persistent_smem_bytes(8, 16) <= 227 * 1024
+                && persistent_smem_bytes(4, 16) <= 227 * 1024 && persistent_smem_bytes(2, 16) <= 227 * 1024,
+              "persistent tile buffers exceed shared memory");
 
 } // namespace gb300

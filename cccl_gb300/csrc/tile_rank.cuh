@@ -1,0 +1,165 @@
+// In-tile digit ranking primitives shared by the onesweep pass and the single-tile sort.
+//
+// A tile is split into warp segments; in round i lane l of warp w holds the key at
+// segment index i*32 + l, so (warp, round, lane) order is source order. Ranking is done
+// in three steps (the structure of CUB's BlockRadixRankMatchEarlyCounts,
+// cub/cub/block/block_radix_rank.cuh:913-1213, with GB300-specific matching):
+//   1. warp_histogram: per-warp digit counts with shared-memory atomics (order-free);
+//   2. block_digit_offsets: per-digit totals, an exclusive scan over warps and over
+//      digits, leaving in whist[w][d] the tile position where warp w's first digit-d key goes;
+//   3. warp_rank_stable: the stable rank of every key among the warp's same-digit keys.
+//
+// Matching on GB300: match.any.sync executes at about one instruction per 64 cycles per SM
+// (measured), so peers are found with one warp ballot per digit bit instead (the
+// technique CUB's warp_matcher_t also uses, cub/cub/util_ptx.cuh:407-446), and the
+// warp's running digit offset is advanced by the highest peer lane with one shared
+// atomic whose result is broadcast with a shuffle.
+#pragma once
+
+#include "sort_common.cuh"
+
+namespace gb300
+{
+
+__device__ __forceinline__ void named_barrier_256()
+{
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t lanemask_le()
+{
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_le;" : "=r"(m));
+  return m;
+}
+
+// Exclusive prefix over the 256 digit slots held by threads [0, 256) (one value per
+// thread). `scratch` holds 8 words. Must be called by exactly threads [0, 256).
+__device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch)
+{
+  const int tid  = threadIdx.x;
+  const int lane = tid & 31;
+  const int w    = tid >> 5;
+  uint32_t x     = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+    {
+      x += y;
+    }
+  }
+  if (lane == 31)
+  {
+    scratch[w] = x;
+  }
+  named_barrier_256();
+  uint32_t pre = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+  {
+    pre += (j < w) ? scratch[j] : 0u;
+  }
+  return pre + x - v;
+}
+
+// Lanes whose 8-bit digit equals this lane's: one ballot per bit. Written in PTX so each
+// bit costs a bit test into a predicate, the vote, a predicated inversion and an AND
+// (measured 1.6x faster on GB300 than the select-based C++ form).
+__device__ __forceinline__ uint32_t warp_match_digit(uint32_t d)
+{
+  uint32_t peers = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b < RADIX_BITS; ++b)
+  {
+    uint32_t bal;
+    asm("{\n"
+        "  .reg .pred p;\n"
+        "  .reg .b32 t;\n"
+        "  and.b32 t, %1, %2;\n"
+        "  setp.ne.u32 p, t, 0;\n"
+        "  vote.ballot.sync.b32 %0, p, 0xffffffff;\n"
+        "  @!p not.b32 %0, %0;\n"
+        "}\n"
+        : "=r"(bal)
+        : "r"(d), "r"(1u << b));
+    peers &= bal;
+  }
+  return peers;
+}
+
+template <class U, bool FP, int ITEMS>
+__device__ __forceinline__ void warp_histogram(const U (&keys)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
+{
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    atomicAdd(&whist_w[extract_digit<U, FP>(keys[i], bit, dmask)], 1u);
+  }
+}
+
+// Threads [0, 256): turns per-warp counts whist[w][d] into tile positions (exclusive over
+// digits, then over warps). Returns this thread's digit total; *tile_start receives the
+// digit's first position in the tile.
+template <int NW>
+__device__ __forceinline__ uint32_t block_digit_offsets(uint32_t* whist, uint32_t* scratch8, uint32_t* tile_start)
+{
+  const int d    = threadIdx.x;
+  uint32_t total = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w)
+  {
+    const uint32_t c        = whist[w * RADIX_DIGITS + d];
+    whist[w * RADIX_DIGITS + d] = total;
+    total += c;
+  }
+  const uint32_t start = digit_exclusive_scan(total, scratch8);
+#pragma unroll
+  for (int w = 0; w < NW; ++w)
+  {
+    whist[w * RADIX_DIGITS + d] += start;
+  }
+  *tile_start = start;
+  return total;
+}
+
+// Stable tile positions: pos[i] = whist_w[d] at the time key i is reached, in source order.
+template <class U, bool FP, int ITEMS>
+__device__ __forceinline__ void warp_rank_stable(
+  const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
+{
+  const int lane    = threadIdx.x & 31;
+  const uint32_t le = lanemask_le();
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t d      = extract_digit<U, FP>(keys[i], bit, dmask);
+    const uint32_t peers  = warp_match_digit(d);
+    const int leader      = 31 - __clz(peers);
+    const uint32_t cnt_le = __popc(peers & le);
+    uint32_t base         = 0;
+    if (lane == leader)
+    {
+      base = atomicAdd(&whist_w[d], cnt_le); // cnt_le of the highest peer = the peer count
+    }
+    // The shuffle completes only after the leader's atomic returned, so the next round's
+    // atomics on the same counter are ordered after this one.
+    base   = __shfl_sync(0xffffffffu, base, leader);
+    pos[i] = base + cnt_le - 1;
+  }
+}
+
+// Order-free tile positions (same digit buckets, arbitrary order inside a bucket).
+template <class U, bool FP, int ITEMS>
+__device__ __forceinline__ void warp_rank_unstable(
+  const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
+{
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    pos[i] = atomicAdd(&whist_w[extract_digit<U, FP>(keys[i], bit, dmask)], 1u);
+  }
+}
+
+} // namespace gb300

@@ -13,10 +13,15 @@
  *      exclusive_sum_kernel          same kernel as histogram_kernel (the scan is fused)
  *      init_bins_and_counters_kernel control-block initialisation
  *      init_lookback_kernel          same kernel as init_bins_and_counters_kernel
- *      onesweep_kernel               one 8-bit digit pass (rank, look-back, scatter)
+ *      onesweep_kernel               one 8-bit digit pass (rank, look-back, scatter); persistent,
+ *                                    bulk-copy prefetch, cooperative launch
+ *      downsweep_kernel              the same pass, one CTA per tile, for buffers that are not
+ *                                    16-byte aligned
  *      single_tile_kernel            whole sort in one CTA for small inputs
- *      upsweep/scan_bins/downsweep (+alt): CUB's multi-pass kernels are never used on
- *      sm_90+; these members alias histogram/exclusive-sum/onesweep so they are non-null.
+ *      alt_downsweep_kernel          first-pass variant for full-width integer keys-only
+ *                                    sorts (order inside a digit bucket is free there)
+ *      upsweep/scan_bins/alt_upsweep: CUB's multi-pass kernels are never used on
+ *      sm_90+; these members alias the histogram kernel so they are non-null.
  *  - runtime_policy: the tile configuration chosen for the key/value types.
  */
 #pragma once
