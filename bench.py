@@ -430,7 +430,24 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", choices=["pairs", "keys"],
+                    help="run two untimed sorts of 2^--log2n keys (u64+u32 pairs or u32 keys) for ncu captures")
+    ap.add_argument("--log2n", type=int, default=24)
     args = ap.parse_args()
+    if args.profile_case:
+        import torch
+
+        ensure_built()
+        n = 1 << args.log2n
+        if args.profile_case == "pairs":
+            s = Sorter(torch, make_inputs(torch, n, "u64"), with_values=True)
+        else:
+            s = Sorter(torch, make_inputs(torch, n, "u32"), with_values=False)
+        s.run()
+        s.run()
+        torch.cuda.synchronize()
+        print(f"profile case {args.profile_case} n=2^{args.log2n} done")
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

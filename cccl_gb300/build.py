@@ -25,6 +25,9 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--use_fast_math"]
+# Tile-shape overrides for tuning builds, e.g. "-DGB300_PERSISTENT_TPB=1024 -DGB300_PERSISTENT_ITEMS=6";
+# applied to the kernels and to the host dispatcher alike.
+TUNE_DEFINES = os.environ.get("GB300_TUNE_DEFINES", "").split()
 
 IMAGES = {
     "radix_k1": "radix_k1.cu",
@@ -64,7 +67,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         CSRC.glob("*.cpp")
     ) + list(INCLUDE.glob("*/*.h")) + list(INCLUDE.glob("*/*/*.h")) + [Path(__file__)]
     stamp = BUILD / "stamp.txt"
-    digest = _digest(sources)
+    digest = _digest(sources) + " ".join(TUNE_DEFINES)
     lib = library_path()
     if not force and lib.exists() and stamp.exists() and stamp.read_text() == digest:
         return lib
@@ -72,7 +75,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     def cubin(name_src):
         name, src = name_src
         out = BUILD / f"{name}.cubin"
-        _run([NVCC, "-cubin", *ARCH, *NVCC_FLAGS, "-I", str(CSRC), str(CSRC / src), "-o", str(out)], verbose)
+        _run([NVCC, "-cubin", *ARCH, *NVCC_FLAGS, *TUNE_DEFINES, "-I", str(CSRC), str(CSRC / src), "-o", str(out)],
+             verbose)
         return out
 
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
@@ -102,7 +106,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     def host_obj(src):
         out = BUILD / (Path(src).stem + ".o")
         _run(
-            [cxx, "-O2", "-fPIC", "-std=c++17", "-DCCCL_C_EXPERIMENTAL", "-fvisibility=hidden", "-Wall", "-I", str(INCLUDE), "-I",
+            [cxx, "-O2", "-fPIC", "-std=c++17", "-DCCCL_C_EXPERIMENTAL", *TUNE_DEFINES, "-fvisibility=hidden", "-Wall", "-I", str(INCLUDE), "-I",
              str(CSRC), "-I", str(CUDA_HOME / "include"), "-c", str(src), "-o", str(out)],
             verbose,
         )

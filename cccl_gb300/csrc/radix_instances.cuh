@@ -13,7 +13,7 @@
   static_assert(gb300::OnesweepSmem<KB, VB, gb300::ONESWEEP_TPB, gb300::onesweep_items(KB, VB)>::bytes          \
                   == gb300::onesweep_smem_bytes(KB, VB),                                                        \
                 "onesweep shared-memory layout mismatch");                                                      \
-  static_assert(gb300::PersistentSmem<KB, VB, gb300::PERSISTENT_TPB, gb300::persistent_items(KB, VB)>::bytes    \
+  static_assert(gb300::PersistentSmem<KB, VB, gb300::persistent_tpb(KB, VB), gb300::persistent_items(KB, VB)>::bytes    \
                   == gb300::persistent_smem_bytes(KB, VB),                                                      \
                 "persistent onesweep shared-memory layout mismatch");                                           \
   extern "C" __global__ void __launch_bounds__(gb300::ONESWEEP_TPB)                                             \
@@ -21,20 +21,20 @@
   {                                                                                                             \
     gb300::onesweep_body<KB, VB, FP, gb300::ONESWEEP_TPB, gb300::onesweep_items(KB, VB), true>(p);              \
   }                                                                                                             \
-  extern "C" __global__ void __launch_bounds__(gb300::PERSISTENT_TPB, 1)                                        \
+  extern "C" __global__ void __launch_bounds__(gb300::persistent_tpb(KB, VB), gb300::PERSISTENT_MINB)                                        \
     gb300_onesweep_k##KB##_v##VB##_##SUF(const gb300::OnesweepParams p)                                         \
   {                                                                                                             \
-    gb300::onesweep_persistent_body<KB, VB, FP, gb300::PERSISTENT_TPB, gb300::persistent_items(KB, VB), true>(p); \
+    gb300::onesweep_persistent_body<KB, VB, FP, gb300::persistent_tpb(KB, VB), gb300::persistent_items(KB, VB), true>(p); \
   }
 
 // First pass of a full-width integer keys-only sort: equal digits may land in any order
 // inside their bucket, because keys equal in that digit are ordered by the later (stable)
 // passes and fully equal integer keys are indistinguishable.
 #define GB300_ONESWEEP_FIRST(KB)                                                                                  \
-  extern "C" __global__ void __launch_bounds__(gb300::PERSISTENT_TPB, 1)                                        \
+  extern "C" __global__ void __launch_bounds__(gb300::persistent_tpb(KB, 0), gb300::PERSISTENT_MINB)                                   \
     gb300_onesweep_first_k##KB##_v0_i(const gb300::OnesweepParams p)                                            \
   {                                                                                                             \
-    gb300::onesweep_persistent_body<KB, 0, false, gb300::PERSISTENT_TPB, gb300::persistent_items(KB, 0), false>(p); \
+    gb300::onesweep_persistent_body<KB, 0, false, gb300::persistent_tpb(KB, 0), gb300::persistent_items(KB, 0), false>(p); \
   }
 
 #define GB300_SINGLE_TILE(KB, VB, FP, SUF)                                                                        \

@@ -29,7 +29,7 @@ RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind)
   p.single_tile_items = SINGLE_TILE_ITEMS;
   p.histogram_tpb     = HISTOGRAM_TPB;
   p.onesweep_smem     = onesweep_smem_bytes(key_bytes, value_bytes);
-  p.persistent_tpb    = PERSISTENT_TPB;
+  p.persistent_tpb    = persistent_tpb(key_bytes, value_bytes);
   p.persistent_items  = persistent_items(key_bytes, value_bytes);
   p.persistent_smem   = persistent_smem_bytes(key_bytes, value_bytes);
   p.single_tile_smem  = single_tile_smem_bytes(key_bytes);

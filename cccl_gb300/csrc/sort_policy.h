@@ -20,7 +20,24 @@ namespace gb300
 {
 
 constexpr int ONESWEEP_TPB     = 384; // CTA-per-tile fallback kernel
-constexpr int PERSISTENT_TPB   = 512; // persistent onesweep kernel (one CTA per SM)
+// Persistent onesweep kernel shape. The GB300_* macros let a tuning build override the
+// shipped table (cccl_gb300/build.py passes GB300_TUNE_DEFINES to both compilers).
+#ifndef GB300_PERSISTENT_MINB
+#  define GB300_PERSISTENT_MINB 1
+#endif
+constexpr int PERSISTENT_MINB = GB300_PERSISTENT_MINB; // CTAs per SM the registers are sized for
+
+// Threads per CTA of the persistent kernel. Tuned on GB300 (2^28 keys): pairs run best
+// with 32 warps of 8 items (more warps hide the ranking latency), keys-only with 16 warps
+// of 20 items (bigger tiles per CTA barrier).
+GB300_HD constexpr int persistent_tpb(int kb, int vb)
+{
+#ifdef GB300_PERSISTENT_TPB
+  return (void) kb, (void) vb, GB300_PERSISTENT_TPB;
+#else
+  return (void) kb, vb > 0 ? 1024 : 512;
+#endif
+}
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
 constexpr int HISTOGRAM_TPB    = 512;
@@ -54,16 +71,36 @@ GB300_HD constexpr size_t onesweep_smem_bytes(int kb, int vb)
 
 // Items per thread of the persistent onesweep kernel: the two tile buffers (keys + values)
 // must fit the 227 KB of shared memory next to the 16 KB of per-warp counters.
+GB300_HD constexpr int persistent_items_nominal(int kb, int vb)
+{
+#ifdef GB300_PERSISTENT_ITEMS
+  return (void) kb, (void) vb, GB300_PERSISTENT_ITEMS;
+#else
+  return vb > 0 ? 8 : kb == 8 ? 16 : kb == 4 ? 20 : 24;
+#endif
+}
+
+GB300_HD constexpr size_t persistent_smem_for(int kb, int vb, int items)
+{
+  return size_t(4) * (persistent_tpb(kb, vb) / 32) * 256 + size_t(8) * 256 + 128
+       + 2 * (round16(size_t(kb) * persistent_tpb(kb, vb) * items)
+              + (vb > 0 ? value_word_bytes(vb) * persistent_tpb(kb, vb) * items : 0));
+}
+
+// Nominal items, reduced until PERSISTENT_MINB CTAs fit in 227 KB of shared memory.
 GB300_HD constexpr int persistent_items(int kb, int vb)
 {
-  return vb >= 16 ? 8 : kb == 8 ? 12 : kb == 4 ? (vb == 0 ? 20 : vb <= 4 ? 16 : 12) : 16;
+  int items = persistent_items_nominal(kb, vb);
+  while (items > 1 && persistent_smem_for(kb, vb, items) * PERSISTENT_MINB > size_t(227) * 1024)
+  {
+    --items;
+  }
+  return items;
 }
 
 GB300_HD constexpr size_t persistent_smem_bytes(int kb, int vb)
 {
-  return size_t(4) * (PERSISTENT_TPB / 32) * 256 + size_t(8) * 256 + 128
-       + 2 * (round16(size_t(kb) * PERSISTENT_TPB * persistent_items(kb, vb))
-              + (vb > 0 ? value_word_bytes(vb) * PERSISTENT_TPB * persistent_items(kb, vb) : 0));
+  return persistent_smem_for(kb, vb, persistent_items(kb, vb));
 }
 
 GB300_HD constexpr int single_tile_capacity()
@@ -93,8 +130,10 @@ GB300_HD constexpr unsigned long long cub_single_tile_limit(int key_bytes, int v
 static_assert(cub_single_tile_limit(4, 0) == 4864, "CUB single-tile cut, 4-byte keys");
 static_assert(cub_single_tile_limit(8, 4) == 2304, "CUB single-tile cut, 8-byte keys");
 static_assert(cub_single_tile_limit(4, 16) == 1024, "CUB single-tile cut, 16-byte values");
-static_assert(persistent_smem_bytes(8, 8) <= 227 * 1024 && persistent_smem_bytes(8, 16) <= 227 * 1024
-                && persistent_smem_bytes(4, 16) <= 227 * 1024 && persistent_smem_bytes(2, 16) <= 227 * 1024,
+static_assert(persistent_smem_bytes(8, 8) * PERSISTENT_MINB <= 227 * 1024
+                && persistent_smem_bytes(8, 16) * PERSISTENT_MINB <= 227 * 1024
+                && persistent_smem_bytes(4, 16) * PERSISTENT_MINB <= 227 * 1024
+                && persistent_smem_bytes(2, 16) * PERSISTENT_MINB <= 227 * 1024,
               "persistent tile buffers exceed shared memory");
 
 } // namespace gb300
