@@ -164,7 +164,10 @@ EXPORTED_SYMBOLS = [
     "cccl_device_segmented_sort_deserialize",
     "cccl_device_segmented_sort_cleanup",
     "cccl_gb300_set_launch_observer",
+    "cccl_gb300_radix_sort_u32_noalloc",
 ]
+
+NOALLOC_MAX_ITEMS = 1 << 20  # CCCL_GB300_NOALLOC_MAX_ITEMS
 
 LAUNCH_OBSERVER = C.CFUNCTYPE(None, C.c_void_p, C.c_char_p, C.c_int, C.c_void_p)
 
@@ -229,6 +232,8 @@ def _declare(lib):
     lib.cccl_serialization_buffer_free.restype = None
     lib.cccl_gb300_set_launch_observer.argtypes = [LAUNCH_OBSERVER, C.c_void_p]
     lib.cccl_gb300_set_launch_observer.restype = None
+    lib.cccl_gb300_radix_sort_u32_noalloc.argtypes = [
+        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_bool, C.c_void_p]
     for name in EXPORTED_SYMBOLS:
         if name not in ("cccl_serialization_buffer_free", "cccl_gb300_set_launch_observer"):
             getattr(lib, name).restype = C.c_int

@@ -37,6 +37,8 @@ IMAGES = {
     "segmented": "segmented_kernels.cu",
 }
 HOST_SOURCES = ["images.cpp", "radix_plan.cpp", "radix_sort_abi.cpp", "segmented_sort_abi.cpp"]
+# Runtime-API translation units (host + device code in one object, linked with static cudart)
+RUNTIME_SOURCES = ["noalloc_sort.cu"]
 
 
 def _digest(paths) -> str:
@@ -112,16 +114,26 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         )
         return out
 
+    def runtime_obj(src):
+        out = BUILD / (Path(src).stem + ".o")
+        _run(
+            [NVCC, "-c", *ARCH, *NVCC_FLAGS, *TUNE_DEFINES, "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+             "-I", str(INCLUDE), "-I", str(CSRC), str(CSRC / src), "-o", str(out)],
+            verbose,
+        )
+        return out
+
     host = [CSRC / s for s in HOST_SOURCES] + [embed]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(host_obj, host))
+        objs = list(ex.map(host_obj, host)) + list(ex.map(runtime_obj, RUNTIME_SOURCES))
 
     libdirs = []
     for d in (CUDA_HOME / "lib64", CUDA_HOME / "lib64" / "stubs", CUDA_HOME / "targets" / "sbsa-linux" / "lib" / "stubs"):
         if d.exists():
             libdirs += ["-L", str(d)]
     tmp = BUILD / (LIB_NAME + ".tmp")
-    _run([cxx, "-shared", "-o", str(tmp), *map(str, objs), *libdirs, "-lcuda", "-Wl,--no-undefined"], verbose)
+    _run([cxx, "-shared", "-o", str(tmp), *map(str, objs), *libdirs, "-lcudart_static", "-lcuda", "-lrt", "-ldl",
+          "-lpthread", "-Wl,--no-undefined"], verbose)
     shutil.move(str(tmp), str(lib))
     stamp.write_text(digest)
     return lib

@@ -276,7 +276,7 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
   constexpr int NW = L::NW;
   constexpr int R  = RADIX_DIGITS;
 
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
   long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
   uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);

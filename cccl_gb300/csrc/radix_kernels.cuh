@@ -208,7 +208,7 @@ __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
   static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
   static_assert(TILE <= 65536, "16-bit source indices");
 
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* whist = reinterpret_cast<uint32_t*>(smem + L::whist_off);
   uint32_t* misc  = reinterpret_cast<uint32_t*>(smem + L::misc_off);
   U* kbuf         = reinterpret_cast<U*>(smem + L::kbuf_off);
