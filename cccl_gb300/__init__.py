@@ -7,6 +7,7 @@ C ABI. There is no CPU fallback: without the built library every call raises.
 
 from .build import build, library_path
 from .radix_sort import DoubleBuffer, SortOrder, make_radix_sort, radix_sort
+from .segmented_sort import make_segmented_sort, segmented_sort
 
 __all__ = [
     "build",
@@ -15,4 +16,6 @@ __all__ = [
     "SortOrder",
     "make_radix_sort",
     "radix_sort",
+    "make_segmented_sort",
+    "segmented_sort",
 ]

@@ -24,7 +24,7 @@ LIB_NAME = "libccclsort.so"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--use_fast_math"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17"]  # no fast-math: comparisons must not flush denormals
 # Tile-shape overrides for tuning builds, e.g. "-DGB300_PERSISTENT_TPB=1024 -DGB300_PERSISTENT_ITEMS=6";
 # applied to the kernels and to the host dispatcher alike.
 TUNE_DEFINES = os.environ.get("GB300_TUNE_DEFINES", "").split()
@@ -34,9 +34,12 @@ IMAGES = {
     "radix_k2": "radix_k2.cu",
     "radix_k4": "radix_k4.cu",
     "radix_k8": "radix_k8.cu",
-    "segmented": "segmented_kernels.cu",
+    "seg_k1": "seg_k1.cu",
+    "seg_k2": "seg_k2.cu",
+    "seg_k4": "seg_k4.cu",
+    "seg_k8": "seg_k8.cu",
 }
-HOST_SOURCES = ["images.cpp", "radix_plan.cpp", "radix_sort_abi.cpp", "segmented_sort_abi.cpp"]
+HOST_SOURCES = ["images.cpp", "radix_plan.cpp", "radix_sort_abi.cpp", "segmented_plan.cpp", "segmented_sort_abi.cpp"]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]
 

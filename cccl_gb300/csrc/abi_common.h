@@ -81,7 +81,7 @@ struct image_ref
   size_t size;
 };
 image_ref radix_image(int key_bytes); // one cubin per key width
-image_ref segmented_image();
+image_ref segmented_image(int key_bytes); // one cubin per key width
 
 // ---- key kinds ----
 enum key_kind : int

@@ -11,7 +11,10 @@ extern const unsigned char gb300_img_radix_k1[], gb300_img_radix_k1_end[];
 extern const unsigned char gb300_img_radix_k2[], gb300_img_radix_k2_end[];
 extern const unsigned char gb300_img_radix_k4[], gb300_img_radix_k4_end[];
 extern const unsigned char gb300_img_radix_k8[], gb300_img_radix_k8_end[];
-extern const unsigned char gb300_img_segmented[], gb300_img_segmented_end[];
+extern const unsigned char gb300_img_seg_k1[], gb300_img_seg_k1_end[];
+extern const unsigned char gb300_img_seg_k2[], gb300_img_seg_k2_end[];
+extern const unsigned char gb300_img_seg_k4[], gb300_img_seg_k4_end[];
+extern const unsigned char gb300_img_seg_k8[], gb300_img_seg_k8_end[];
 }
 
 namespace gb300
@@ -34,9 +37,21 @@ image_ref radix_image(int key_bytes)
   }
 }
 
-image_ref segmented_image()
+image_ref segmented_image(int key_bytes)
 {
-  return {gb300_img_segmented, size_t(gb300_img_segmented_end - gb300_img_segmented)};
+  switch (key_bytes)
+  {
+    case 1:
+      return {gb300_img_seg_k1, size_t(gb300_img_seg_k1_end - gb300_img_seg_k1)};
+    case 2:
+      return {gb300_img_seg_k2, size_t(gb300_img_seg_k2_end - gb300_img_seg_k2)};
+    case 4:
+      return {gb300_img_seg_k4, size_t(gb300_img_seg_k4_end - gb300_img_seg_k4)};
+    case 8:
+      return {gb300_img_seg_k8, size_t(gb300_img_seg_k8_end - gb300_img_seg_k8)};
+    default:
+      throw cuda_error(CUDA_ERROR_NOT_SUPPORTED, "no segmented kernels for this key width");
+  }
 }
 
 } // namespace gb300

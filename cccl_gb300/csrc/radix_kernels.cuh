@@ -196,8 +196,20 @@ struct SingleTileSmem
   static constexpr size_t bytes     = ibuf_off + 2 * sizeof(uint16_t) * TILE;
 };
 
+// Sorts n <= TPB*ITEMS keys (and values) by bits [begin_bit, end_bit) inside one CTA.
+// Reads keys_in/values_in, writes keys_out/values_out (which may alias the inputs: all
+// reads complete before the first write). Starts with a CTA barrier so a persistent CTA
+// can call it for one segment after another.
 template <int KB, int VB, bool FP, int TPB, int ITEMS>
-__device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
+__device__ __forceinline__ void block_sort_body(
+  const void* keys_in,
+  void* keys_out,
+  const void* values_in,
+  void* values_out,
+  uint32_t num_items,
+  int begin_bit,
+  int end_bit,
+  const KeyCodec& codec)
 {
   using L            = SingleTileSmem<KB, TPB, ITEMS>;
   using U            = typename L::U;
@@ -217,19 +229,20 @@ __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
   const int tid    = threadIdx.x;
   const int lane   = tid & 31;
   const int warp   = tid >> 5;
-  const uint32_t n = p.num_items;
-  const U* kin     = static_cast<const U*>(p.keys_in);
+  const uint32_t n = num_items;
+  const U* kin     = static_cast<const U*>(keys_in);
 
+  __syncthreads();
   for (int s = tid; s < TILE; s += TPB)
   {
-    kbuf[s] = (uint32_t(s) < n) ? encode_key<U>(kin[s], p.codec) : U(~U(0));
+    kbuf[s] = (uint32_t(s) < n) ? encode_key<U>(kin[s], codec) : U(~U(0));
     ibuf[s] = uint16_t(s);
   }
 
   int cur = 0;
-  for (int bit = p.begin_bit; bit < p.end_bit; bit += RADIX_BITS)
+  for (int bit = begin_bit; bit < end_bit; bit += RADIX_BITS)
   {
-    const uint32_t dmask = (1u << min(RADIX_BITS, p.end_bit - bit)) - 1u;
+    const uint32_t dmask = (1u << min(RADIX_BITS, end_bit - bit)) - 1u;
     for (int i = tid; i < NW * R; i += TPB)
     {
       whist[i] = 0;
@@ -268,17 +281,45 @@ __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
     cur ^= 1;
   }
 
-  U* kout             = static_cast<U*>(p.keys_out);
-  const U* kfin       = kbuf + cur * TILE;
+  U* kout              = static_cast<U*>(keys_out);
+  const U* kfin        = kbuf + cur * TILE;
   const uint16_t* ifin = ibuf + cur * TILE;
-  for (uint32_t s = tid; s < n; s += TPB)
+  if constexpr (VB > 0)
   {
-    kout[s] = decode_key<U>(kfin[s], p.codec);
-    if constexpr (VB > 0)
+    // values may alias their source: gather into registers before any store
+    constexpr int PER = (TILE + TPB - 1) / TPB;
+    V vtmp[PER];
+#pragma unroll
+    for (int j = 0; j < PER; ++j)
     {
-      static_cast<V*>(p.values_out)[s] = static_cast<const V*>(p.values_in)[ifin[s]];
+      const uint32_t s = j * TPB + tid;
+      if (s < n)
+      {
+        vtmp[j] = static_cast<const V*>(values_in)[ifin[s]];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PER; ++j)
+    {
+      const uint32_t s = j * TPB + tid;
+      if (s < n)
+      {
+        static_cast<V*>(values_out)[s] = vtmp[j];
+      }
     }
   }
+  for (uint32_t s = tid; s < n; s += TPB)
+  {
+    kout[s] = decode_key<U>(kfin[s], codec);
+  }
+}
+
+template <int KB, int VB, bool FP, int TPB, int ITEMS>
+__device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
+{
+  block_sort_body<KB, VB, FP, TPB, ITEMS>(
+    p.keys_in, p.keys_out, p.values_in, p.values_out, p.num_items, p.begin_bit, p.end_bit, p.codec);
 }
 
 } // namespace gb300

@@ -1,0 +1,734 @@
+// Batched segmented sort kernels (cub::DeviceSegmentedSort semantics) for sm_103a.
+//
+// One call sorts every segment [begin[i], end[i]) of the keys (and values) in place of
+// cub::DeviceSegmentedSort (cub/cub/device/dispatch/dispatch_segmented_sort.cuh). The work
+// is split on the device, with no host round trip (the reference copies partition sizes to
+// the host and synchronizes, dispatch_segmented_sort.cuh:883-895):
+//   * seg_classify bins every segment into a size class and appends it to that class's
+//     list (warp-aggregated atomics); large segments also get a contiguous range of tiles;
+//   * warp class, size <= medium tile: a sub-warp of T lanes runs CUB's merge network for
+//     that size (cub/cub/agent/agent_sub_warp_merge_sort.cuh:225-340,
+//     cub/cub/block/block_merge_sort.cuh:39-160,425-520, cub/cub/thread/thread_sort.cuh:27-50)
+//     with the key type's own operator<; this is what decides where NaN keys land, so it
+//     is reproduced step for step;
+//   * block class: one CTA sorts the segment in shared memory with stable 8-bit passes;
+//   * device class: all large segments together run the onesweep machinery, one launch per
+//     digit pass over every large segment's tiles, each segment with its own look-back
+//     chain and digit bases (CUB sorts each large segment with a single CTA,
+//     kernel_segmented_sort.cuh:430-573).
+// Every class kernel is persistent (grid sized to the GPU, work taken from the lists), so
+// the host never needs the class sizes.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "onesweep.cuh"
+#include "radix_kernels.cuh"
+
+namespace gb300
+{
+
+enum : uint32_t
+{
+  SEG_CTR_SMALL = 0,
+  SEG_CTR_MEDIUM,
+  SEG_CTR_BLOCK_S,
+  SEG_CTR_BLOCK_L,
+  SEG_CTR_DEVICE,
+  SEG_CTR_DEVICE_TILES,
+  SEG_CTR_TICKET_SMALL,
+  SEG_CTR_TICKET_MEDIUM,
+  SEG_CTR_TICKET_BLOCK_S,
+  SEG_CTR_TICKET_BLOCK_L,
+  SEG_CTR_TICKET_HIST,
+  SEG_CTR_TICKET_SCAN,
+  SEG_CTR_TICKET_PASS0, // one per device pass
+  SEG_CTR_COUNT = SEG_CTR_TICKET_PASS0 + 16
+};
+
+__device__ __forceinline__ long long load_offset(const void* p, unsigned long long i, int wide)
+{
+  return wide ? static_cast<const long long*>(p)[i] : (long long) static_cast<const int*>(p)[i];
+}
+
+// Appends `item` to list[counter] with one atomic per warp and list.
+__device__ __forceinline__ void warp_append(bool take, uint32_t* counter, uint32_t* list, uint32_t item)
+{
+  const uint32_t m = __ballot_sync(0xffffffffu, take);
+  if (!take)
+  {
+    return;
+  }
+  const int lane    = threadIdx.x & 31;
+  const int leader  = __ffs(m) - 1;
+  uint32_t base     = 0;
+  if (lane == leader)
+  {
+    base = atomicAdd(counter, uint32_t(__popc(m)));
+  }
+  base = __shfl_sync(m, base, leader);
+  list[base + __popc(m & ((1u << lane) - 1u))] = item;
+}
+
+__device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
+{
+  const unsigned long long stride = (unsigned long long) gridDim.x * blockDim.x;
+  const unsigned long long n_round = (p.num_segments + 31) / 32 * 32; // whole warps take part in the ballots
+  for (unsigned long long s = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; s < n_round; s += stride)
+  {
+    long long b = 0, size = 0;
+    if (s < p.num_segments)
+    {
+      b    = load_offset(p.begin_offsets, s, p.offsets_64);
+      size = load_offset(p.end_offsets, s, p.offsets_64) - b;
+    }
+    int cls = -1; // 0 small, 1 medium, 2 block small, 3 block large, 4 device
+    if (size > 0 && (b < 0 || (unsigned long long) (b + size) > p.num_items))
+    {
+      atomicOr(p.status, STATUS_BAD_SEGMENT); // outside the keys: not sorted, never touched
+      size = 0;
+    }
+    if (size > 0)
+    {
+      if (size <= p.medium_tile)
+      {
+        cls = (p.partition && size <= p.small_tile) ? 0 : 1;
+      }
+      else if (size <= p.block_small_cap)
+      {
+        cls = 2;
+      }
+      else if (size <= p.block_large_cap)
+      {
+        cls = 3;
+      }
+      else
+      {
+        cls = 4;
+      }
+      if (cls == 4 && size >= (1ll << 30))
+      {
+        atomicOr(p.status, STATUS_BAD_SEGMENT); // look-back counts hold 30 bits
+        cls = -1;
+      }
+    }
+    warp_append(cls == 0, p.counters + SEG_CTR_SMALL, p.small_list, uint32_t(s));
+    warp_append(cls == 1, p.counters + SEG_CTR_MEDIUM, p.medium_list, uint32_t(s));
+    warp_append(cls == 2, p.counters + SEG_CTR_BLOCK_S, p.block_s_list, uint32_t(s));
+    warp_append(cls == 3, p.counters + SEG_CTR_BLOCK_L, p.block_l_list, uint32_t(s));
+    if (cls == 4)
+    {
+      const uint32_t tiles = uint32_t((size + p.device_tile - 1) / p.device_tile);
+      const uint32_t idx   = atomicAdd(p.counters + SEG_CTR_DEVICE, 1u);
+      const uint32_t base  = atomicAdd(p.counters + SEG_CTR_DEVICE_TILES, tiles);
+      if (idx < p.max_device_segments && (unsigned long long) base + tiles <= p.max_tiles)
+      {
+        p.device_list[idx] = DeviceSegment{(unsigned long long) b, uint32_t(size), base};
+        for (uint32_t t = 0; t < tiles; ++t)
+        {
+          p.tile_segment[base + t] = idx;
+        }
+      }
+      else
+      {
+        atomicOr(p.status, STATUS_SEG_CAPACITY); // overlapping segments exceed the plan
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// warp class: CUB's sub-warp merge sort, T lanes x I items per segment
+// ---------------------------------------------------------------------------------------
+template <int BYTES>
+struct signed_of;
+template <>
+struct signed_of<1>
+{
+  using type = signed char;
+};
+template <>
+struct signed_of<2>
+{
+  using type = short;
+};
+template <>
+struct signed_of<4>
+{
+  using type = int;
+};
+template <>
+struct signed_of<8>
+{
+  using type = long long;
+};
+
+template <int KB, int KIND>
+struct NativeKey
+{
+  using U = typename uint_of<KB>::type;
+  __device__ static bool less(U a, U b)
+  {
+    if constexpr (KIND == 0)
+    {
+      return a < b;
+    }
+    else if constexpr (KIND == 1)
+    {
+      using S = typename signed_of<KB>::type;
+      return S(a) < S(b);
+    }
+    else if constexpr (KB == 2)
+    {
+      return __hlt(__ushort_as_half(a), __ushort_as_half(b));
+    }
+    else if constexpr (KB == 4)
+    {
+      return __uint_as_float(a) < __uint_as_float(b);
+    }
+    else
+    {
+      return __longlong_as_double((long long) a) < __longlong_as_double((long long) b);
+    }
+  }
+  __device__ static bool equal(U a, U b)
+  {
+    if constexpr (KIND != 2)
+    {
+      return a == b;
+    }
+    else if constexpr (KB == 2)
+    {
+      return __heq(__ushort_as_half(a), __ushort_as_half(b));
+    }
+    else if constexpr (KB == 4)
+    {
+      return __uint_as_float(a) == __uint_as_float(b);
+    }
+    else
+    {
+      return __longlong_as_double((long long) a) == __longlong_as_double((long long) b);
+    }
+  }
+};
+
+template <int KB, int KIND>
+struct NetworkCompare
+{
+  using U = typename uint_of<KB>::type;
+  bool descending;
+  __device__ bool operator()(U a, U b) const
+  {
+    return descending ? NativeKey<KB, KIND>::less(b, a) : NativeKey<KB, KIND>::less(a, b);
+  }
+};
+
+// Bit pattern CUB loads past the end of a segment: the raw key that encodes to all ones
+// (ascending) or all zeros (descending).
+template <int KB, int KIND>
+__device__ __forceinline__ typename uint_of<KB>::type network_oob(bool descending)
+{
+  using U      = typename uint_of<KB>::type;
+  const U all  = U(~U(0));
+  const U high = high_bit<U>();
+  if constexpr (KIND == 0)
+  {
+    return descending ? U(0) : all;
+  }
+  else if constexpr (KIND == 1)
+  {
+    return descending ? high : U(all ^ high);
+  }
+  else
+  {
+    return descending ? all : U(all ^ high);
+  }
+}
+
+template <int KB, int KIND, int VB, int T, int I>
+struct NetworkSmem
+{
+  using U                      = typename uint_of<KB>::type;
+  using V                      = typename value_word<VB>::type;
+  static constexpr int TILE    = T * I;
+  static constexpr int GROUPS  = 32 / T; // sub-warps per warp
+  static constexpr size_t kgrp = ((sizeof(U) * (TILE + 1) + 15) / 16) * 16;
+  static constexpr size_t vgrp = VB > 0 ? ((sizeof(V) * (TILE + 1) + 15) / 16) * 16 : 0;
+  static constexpr size_t per_warp = GROUPS * (kgrp + vgrp);
+};
+
+// One sub-warp sorts one segment of `size` keys at `kin` into `kout` (may alias).
+template <int KB, int KIND, int VB, int T, int I>
+__device__ __forceinline__ void network_sort_segment(
+  const typename uint_of<KB>::type* kin,
+  typename uint_of<KB>::type* kout,
+  const typename value_word<VB>::type* vin,
+  typename value_word<VB>::type* vout,
+  int size,
+  bool descending,
+  typename uint_of<KB>::type* kshared,
+  typename value_word<VB>::type* vshared,
+  uint32_t member_mask,
+  int l) // lane within the sub-warp
+{
+  using U         = typename uint_of<KB>::type;
+  using V         = typename value_word<VB>::type;
+  constexpr int TILE = T * I;
+  const NetworkCompare<KB, KIND> op{descending};
+
+  if (size < 3)
+  {
+    // short circuit: only the sub-warp's first lane works
+    if (l == 0)
+    {
+      if (size == 1)
+      {
+        const U k0 = kin[0];
+        V v0{};
+        if constexpr (VB > 0)
+        {
+          v0 = vin[0];
+        }
+        kout[0] = k0;
+        if constexpr (VB > 0)
+        {
+          vout[0] = v0;
+        }
+      }
+      else
+      {
+        const U lhs       = kin[0];
+        const U rhs       = kin[1];
+        const bool keep   = NativeKey<KB, KIND>::equal(lhs, rhs) || op(lhs, rhs);
+        V lv{}, rv{};
+        if constexpr (VB > 0)
+        {
+          lv = vin[0];
+          rv = vin[1];
+        }
+        kout[0] = keep ? lhs : rhs;
+        kout[1] = keep ? rhs : lhs;
+        if constexpr (VB > 0)
+        {
+          vout[0] = keep ? lv : rv;
+          vout[1] = keep ? rv : lv;
+        }
+      }
+    }
+    return;
+  }
+
+  const U oob = network_oob<KB, KIND>(descending);
+  U keys[I];
+  V vals[VB > 0 ? I : 1];
+#pragma unroll
+  for (int i = 0; i < I; ++i)
+  {
+    const int x = l * I + i;
+    keys[i]     = x < size ? kin[x] : oob;
+    if constexpr (VB > 0)
+    {
+      if (x < size)
+      {
+        vals[i] = vin[x];
+      }
+    }
+  }
+  // past the valid items: the lane's running maximum (its first item excluded)
+  {
+    U max_key = oob;
+#pragma unroll
+    for (int i = 1; i < I; ++i)
+    {
+      if (l * I + i < size)
+      {
+        max_key = op(max_key, keys[i]) ? keys[i] : max_key;
+      }
+      else
+      {
+        keys[i] = max_key;
+      }
+    }
+  }
+  // stable odd-even transposition sort inside the lane
+  if (l * I < size)
+  {
+#pragma unroll
+    for (int i = 0; i < I; ++i)
+    {
+#pragma unroll
+      for (int j = 1 & i; j < I - 1; j += 2)
+      {
+        if (op(keys[j + 1], keys[j]))
+        {
+          const U t = keys[j];
+          keys[j]   = keys[j + 1];
+          keys[j + 1] = t;
+          if constexpr (VB > 0)
+          {
+            const V tv  = vals[j];
+            vals[j]     = vals[j + 1];
+            vals[j + 1] = tv;
+          }
+        }
+      }
+    }
+  }
+  // merge rounds through shared memory
+#pragma unroll 1
+  for (int target = 2; target <= T; target *= 2)
+  {
+    const int merged = target / 2;
+    const int mask   = target - 1;
+    __syncwarp(member_mask);
+#pragma unroll
+    for (int i = 0; i < I; ++i)
+    {
+      kshared[l * I + i] = keys[i];
+    }
+    __syncwarp(member_mask);
+    const int start  = I * (~mask & l);
+    const int span   = I * merged;
+    const int diag   = min(size, I * (mask & l));
+    const int k1_beg = min(size, start);
+    const int k1_end = min(size, k1_beg + span);
+    const int k2_beg = k1_end;
+    const int k2_end = min(size, k2_beg + span);
+    const int n1     = k1_end - k1_beg;
+    const int n2     = k2_end - k2_beg;
+    int lo           = diag < n2 ? 0 : diag - n2;
+    int hi           = min(diag, n1);
+    while (lo < hi)
+    {
+      const int mid = lo + (hi - lo) / 2;
+      if (op(kshared[k2_beg + diag - 1 - mid], kshared[k1_beg + mid]))
+      {
+        hi = mid;
+      }
+      else
+      {
+        lo = mid + 1;
+      }
+    }
+    int b1       = k1_beg + lo;
+    int b2       = k2_beg + diag - lo;
+    const int e1 = k1_end;
+    const int e2 = k2_end;
+    U key1       = (e1 - b1) != 0 ? kshared[b1] : oob;
+    U key2       = (e2 - b2) != 0 ? kshared[b2] : oob;
+    int idx[I]; // may point past the valid items for outputs past them (never stored)
+#pragma unroll
+    for (int i = 0; i < I; ++i)
+    {
+      const bool p = (b2 < e2) && ((b1 >= e1) || op(key2, key1));
+      keys[i]      = p ? key2 : key1;
+      idx[i]       = p ? b2++ : b1++;
+      if (p)
+      {
+        key2 = kshared[min(b2, TILE)];
+      }
+      else
+      {
+        key1 = kshared[min(b1, TILE)];
+      }
+    }
+    if constexpr (VB > 0)
+    {
+      __syncwarp(member_mask);
+#pragma unroll
+      for (int i = 0; i < I; ++i)
+      {
+        vshared[l * I + i] = vals[i];
+      }
+      __syncwarp(member_mask);
+#pragma unroll
+      for (int i = 0; i < I; ++i)
+      {
+        vals[i] = vshared[min(idx[i], TILE)];
+      }
+    }
+  }
+  __syncwarp(member_mask);
+#pragma unroll
+  for (int i = 0; i < I; ++i)
+  {
+    const int x = l * I + i;
+    if (x < size)
+    {
+      kout[x] = keys[i];
+      if constexpr (VB > 0)
+      {
+        vout[x] = vals[i];
+      }
+    }
+  }
+}
+
+// Persistent: each sub-warp takes segments from `list` until it is exhausted.
+template <int KB, int KIND, int VB, int T, int I>
+__device__ __forceinline__ void seg_network_body(const SegSortParams& p, const uint32_t* list, uint32_t count_index,
+                                                 uint32_t ticket_index)
+{
+  using L      = NetworkSmem<KB, KIND, VB, T, I>;
+  using U      = typename L::U;
+  using V      = typename L::V;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int warp   = threadIdx.x >> 5;
+  const int lane   = threadIdx.x & 31;
+  const int group  = lane / T;
+  const int l      = lane % T;
+  const uint32_t member_mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (group * T));
+  unsigned char* wbase = smem + warp * L::per_warp;
+  U* kshared           = reinterpret_cast<U*>(wbase + group * L::kgrp);
+  V* vshared           = reinterpret_cast<V*>(wbase + L::GROUPS * L::kgrp + group * L::vgrp);
+
+  const uint32_t count = p.counters[count_index];
+  while (true)
+  {
+    // one ticket per warp covers GROUPS segments
+    uint32_t first = 0;
+    if (lane == 0)
+    {
+      first = atomicAdd(p.counters + ticket_index, uint32_t(L::GROUPS));
+    }
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if (first >= count)
+    {
+      break;
+    }
+    const uint32_t item = first + group;
+    if (item < count)
+    {
+      const uint32_t s   = list[item];
+      const long long b  = load_offset(p.begin_offsets, s, p.offsets_64);
+      const int size     = int(load_offset(p.end_offsets, s, p.offsets_64) - b);
+      network_sort_segment<KB, KIND, VB, T, I>(
+        static_cast<const U*>(p.keys_in) + b,
+        static_cast<U*>(p.keys_out) + b,
+        VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
+        VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
+        size,
+        p.descending != 0,
+        kshared,
+        vshared,
+        member_mask,
+        l);
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// block class: one CTA per segment, shared-memory LSD passes
+// ---------------------------------------------------------------------------------------
+template <int KB, int VB, bool FP, int TPB, int ITEMS>
+__device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uint32_t* list, uint32_t count_index,
+                                               uint32_t ticket_index)
+{
+  using U = typename uint_of<KB>::type;
+  using V = typename value_word<VB>::type;
+  __shared__ uint32_t ticket;
+  const uint32_t count = p.counters[count_index];
+  while (true)
+  {
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      ticket = atomicAdd(p.counters + ticket_index, 1u);
+    }
+    __syncthreads();
+    const uint32_t item = ticket;
+    if (item >= count)
+    {
+      break;
+    }
+    const uint32_t s  = list[item];
+    const long long b = load_offset(p.begin_offsets, s, p.offsets_64);
+    const uint32_t n  = uint32_t(load_offset(p.end_offsets, s, p.offsets_64) - b);
+    block_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
+                                            static_cast<U*>(p.keys_out) + b,
+                                            VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
+                                            VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
+                                            n,
+                                            0,
+                                            8 * KB,
+                                            p.codec);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// device class: all large segments together
+// ---------------------------------------------------------------------------------------
+// Per-segment digit counts of every pass (one read of the large segments), and the
+// clearing of pass 0's look-back rows.
+template <int KB, bool FP, int TPB>
+__device__ __forceinline__ void seg_device_histogram_body(const SegDeviceParams& p)
+{
+  using U         = typename uint_of<KB>::type;
+  constexpr int R = RADIX_DIGITS;
+  __shared__ uint32_t sh[SEG_MAX_PASSES * R]; // up to 8 digits plus one split pass
+  __shared__ uint32_t ticket;
+  // with overlapping segments the lists may be incomplete: do no large-segment work at all
+  const uint32_t ntiles = (*p.status & STATUS_SEG_CAPACITY) ? 0u : p.counters[SEG_CTR_DEVICE_TILES];
+  const int tid         = threadIdx.x;
+
+  for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < (unsigned long long) ntiles * R;
+       i += (unsigned long long) gridDim.x * TPB)
+  {
+    p.lookback[0][i] = 0u;
+  }
+  while (true)
+  {
+    __syncthreads();
+    if (tid == 0)
+    {
+      ticket = atomicAdd(p.counters + SEG_CTR_TICKET_HIST, 1u);
+    }
+    for (int i = tid; i < p.num_passes * R; i += TPB)
+    {
+      sh[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t t = ticket;
+    if (t >= ntiles)
+    {
+      break;
+    }
+    const uint32_t si        = p.tile_segment[t];
+    const DeviceSegment seg  = p.device_list[si];
+    const uint32_t local     = t - seg.tile_base;
+    const uint32_t first     = local * p.device_tile;
+    const uint32_t valid     = min(p.device_tile, seg.size - first);
+    const U* keys            = static_cast<const U*>(p.keys_in) + seg.begin + first;
+    for (uint32_t i = tid; i < valid; i += TPB)
+    {
+      const U k = encode_key<U>(keys[i], p.codec);
+      for (int q = 0; q < p.num_passes; ++q)
+      {
+        const int b  = p.pass_bit[q];
+        const int nb = p.pass_bits[q];
+        atomicAdd(&sh[q * R + extract_digit<U, FP>(k, b, (1u << nb) - 1u)], 1u);
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < p.num_passes * R; i += TPB)
+    {
+      if (sh[i] != 0)
+      {
+        atomicAdd(&p.seg_counts[(size_t) si * p.num_passes * R + i], sh[i]);
+      }
+    }
+  }
+}
+
+// Per large segment: digit bases of every pass = segment begin + exclusive digit prefix.
+template <int TPB>
+__device__ __forceinline__ void seg_device_scan_body(const SegDeviceParams& p)
+{
+  constexpr int R = RADIX_DIGITS;
+  static_assert(TPB == R, "one thread per digit");
+  __shared__ uint32_t scratch[8];
+  __shared__ uint32_t ticket;
+  const uint32_t nseg = (*p.status & STATUS_SEG_CAPACITY) ? 0u : p.counters[SEG_CTR_DEVICE];
+  while (true)
+  {
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      ticket = atomicAdd(p.counters + SEG_CTR_TICKET_SCAN, 1u);
+    }
+    __syncthreads();
+    const uint32_t si = ticket;
+    if (si >= nseg)
+    {
+      break;
+    }
+    const unsigned long long begin = p.device_list[si].begin;
+    for (int q = 0; q < p.num_passes; ++q)
+    {
+      const size_t row = ((size_t) si * p.num_passes + q) * R;
+      const uint32_t c = p.seg_counts[row + threadIdx.x];
+      const uint32_t e = digit_exclusive_scan(c, scratch);
+      p.seg_bins[row + threadIdx.x] = begin + e;
+      named_barrier_256(); // scratch is reused by the next pass's scan
+    }
+  }
+}
+
+// One digit pass over all large segments: CTAs take tiles in ticket order (forward progress:
+// a tile only waits on lower tiles of its own segment, already taken by running CTAs).
+template <int KB, int VB, bool FP, int TPB, int ITEMS>
+__device__ __forceinline__ void seg_device_onesweep_body(const SegDeviceParams& dp)
+{
+  const int pass = dp.pass;
+  using L          = OnesweepSmem<KB, VB, TPB, ITEMS>;
+  using U          = typename L::U;
+  using V          = typename L::V;
+  constexpr int NW = L::NW;
+  constexpr int R  = RADIX_DIGITS;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
+  long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
+  uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);
+  U* kstage         = reinterpret_cast<U*>(smem + L::kstage_off);
+  V* vstage         = reinterpret_cast<V*>(smem + L::vstage_off);
+
+  const uint32_t ntiles = (*dp.status & STATUS_SEG_CAPACITY) ? 0u : dp.counters[SEG_CTR_DEVICE_TILES];
+  const int tid         = threadIdx.x;
+  while (true)
+  {
+    __syncthreads();
+    if (tid == 0)
+    {
+      misc[0] = atomicAdd(dp.counters + SEG_CTR_TICKET_PASS0 + pass, 1u);
+      misc[1] = 0u;
+    }
+    for (int i = tid; i < NW * R; i += TPB)
+    {
+      whist[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t t = misc[0];
+    if (t >= ntiles)
+    {
+      break;
+    }
+    const uint32_t si       = dp.tile_segment[t];
+    const DeviceSegment seg = dp.device_list[si];
+
+    OnesweepParams p{};
+    p.keys_in         = static_cast<const U*>(dp.keys_src[pass]) + seg.begin;
+    p.keys_out        = dp.keys_dst[pass];
+    p.values_in       = VB > 0 ? static_cast<const V*>(dp.values_src[pass]) + seg.begin : nullptr;
+    p.values_out      = dp.values_dst[pass];
+    p.num_items_total = dp.num_items;
+    p.portion_items   = seg.size;
+    p.portion_tiles   = (seg.size + dp.device_tile - 1) / dp.device_tile;
+    p.tile_row_base   = seg.tile_base;
+    p.lookback        = dp.lookback[pass & 1];
+    p.lookback_next   = (pass + 1 < dp.num_passes) ? dp.lookback[(pass + 1) & 1] : nullptr;
+    p.bins            = dp.seg_bins + ((size_t) si * dp.num_passes + pass) * R;
+    p.bins_next       = nullptr;
+    p.status          = dp.status;
+    p.codec           = dp.codec;
+    p.current_bit     = dp.pass_bit[pass];
+    p.num_bits        = dp.pass_bits[pass];
+    p.encode_in       = pass == 0;
+    p.decode_out      = pass == dp.num_passes - 1;
+
+    const uint32_t local      = t - seg.tile_base;
+    const uint32_t tile_first = local * L::TILE;
+    const uint32_t valid      = min(uint32_t(L::TILE), seg.size - tile_first);
+    U keys[ITEMS];
+    load_tile_keys_global<KB, TPB, ITEMS>(p, tile_first, valid, keys);
+    onesweep_tile<KB, VB, FP, TPB, ITEMS, true>(p, local, valid, keys, whist, gdelta, misc, kstage, vstage, [&](auto& vals) {
+      if constexpr (VB > 0)
+      {
+        load_tile_values_global<VB, TPB, ITEMS>(p, tile_first, valid, vals);
+      }
+    });
+  }
+}
+
+} // namespace gb300

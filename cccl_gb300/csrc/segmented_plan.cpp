@@ -1,0 +1,282 @@
+// Host dispatcher of the batched segmented sort (see segmented_plan.h).
+//
+// Reference: cub/cub/device/dispatch/dispatch_segmented_sort.cuh
+//   temp-storage layout and size query            :459-574
+//   buffer routing, final selector                :579-669, :722-746
+//   partitioning threshold (> 500 segments)       :465
+// The large-segment passes use 8-bit digits (CUB uses 6-bit ones); when the caller allows
+// overwriting, the pass count is adjusted by splitting one digit so the result lands in the
+// same buffer CUB's 6-bit pass count selects, and the returned selector is CUB's.
+#include "segmented_plan.h"
+
+#include <algorithm>
+
+#include "abi_common.h"
+#include "sort_policy.h"
+
+namespace gb300
+{
+
+namespace
+{
+uint64_t ceil_div(uint64_t a, uint64_t b)
+{
+  return (a + b - 1) / b;
+}
+
+constexpr uint32_t SEG_COUNTERS = 32; // counters + status, see segmented_kernels.cuh
+} // namespace
+
+SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
+{
+  SegmentedPolicy p{};
+  p.key_bytes           = kb;
+  p.value_bytes         = vb;
+  p.key_kind            = kind;
+  p.small_threads       = seg_small_threads(kb, vb);
+  p.small_items         = seg_small_items(kb, vb);
+  p.medium_threads      = seg_medium_threads(kb, vb);
+  p.medium_items        = seg_medium_items(kb, vb);
+  p.block_s_cap         = SEG_BLOCK_S_TPB * SEG_BLOCK_S_ITEMS;
+  p.block_l_cap         = SEG_BLOCK_L_TPB * SEG_BLOCK_L_ITEMS;
+  p.pass_tpb            = SEG_PASS_TPB;
+  p.pass_items          = onesweep_items(kb, vb);
+  p.network_small_smem  = seg_network_smem(kb, vb, p.small_threads, p.small_items);
+  p.network_medium_smem = seg_network_smem(kb, vb, p.medium_threads, p.medium_items);
+  p.block_s_smem        = block_sort_smem(kb, SEG_BLOCK_S_TPB, SEG_BLOCK_S_ITEMS);
+  p.block_l_smem        = block_sort_smem(kb, SEG_BLOCK_L_TPB, SEG_BLOCK_L_ITEMS);
+  p.pass_smem           = onesweep_smem_bytes(kb, vb);
+  return p;
+}
+
+void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels& ks, const SegmentedCall& c,
+                             int* selector)
+{
+  const int kb        = pol.key_bytes;
+  const int vb        = pol.value_bytes;
+  const bool has_vals = vb > 0 && c.values[0] != nullptr;
+  const uint64_t n    = c.num_items;
+  const uint64_t nseg = c.num_segments;
+  *selector           = 0;
+
+  // ---- digit passes of the large segments and the buffer that receives the result ----
+  const int pass6_count = int(ceil_div(uint64_t(8 * kb), kb > 1 ? 6 : 4)); // CUB's radix passes
+  const int target      = c.overwrite ? (pass6_count & 1) : 1;
+  int bit[SEG_MAX_PASSES];
+  int bits[SEG_MAX_PASSES];
+  int passes = 0;
+  for (int b = 0; b < 8 * kb; b += RADIX_BITS)
+  {
+    bit[passes]  = b;
+    bits[passes] = RADIX_BITS;
+    ++passes;
+  }
+  if (c.overwrite && (passes & 1) != target)
+  {
+    // split the last digit into two 4-bit passes: the parity now matches CUB's
+    bits[passes - 1] = 4;
+    bit[passes]      = bit[passes - 1] + 4;
+    bits[passes]     = 4;
+    ++passes;
+  }
+
+  // ---- temporary storage ----
+  const uint64_t pass_tile = uint64_t(pol.pass_tpb) * pol.pass_items;
+  const uint64_t max_dev   = std::min<uint64_t>(nseg, n / (uint64_t(pol.block_l_cap) + 1));
+  const uint64_t max_tiles = ceil_div(n, pass_tile) + max_dev;
+  const bool need_tmp      = !c.overwrite && passes > 1 && max_dev > 0;
+
+  size_t off               = 0;
+  const size_t ctrl_off    = off;
+  off += align_up(4 * SEG_COUNTERS, 256);
+  const size_t counts_off  = off;
+  off += align_up(4 * size_t(max_dev) * passes * RADIX_DIGITS, 256);
+  const size_t zero_bytes  = off; // control block + per-segment counts are zeroed per call
+  const size_t lists_off   = off;
+  off += 4 * align_up(4 * size_t(nseg), 256);
+  const size_t dev_off     = off;
+  off += align_up(sizeof(DeviceSegment) * size_t(max_dev), 256);
+  const size_t tseg_off    = off;
+  off += align_up(4 * size_t(max_tiles), 256);
+  const size_t bins_off    = off;
+  off += align_up(8 * size_t(max_dev) * passes * RADIX_DIGITS, 256);
+  const size_t lb_off      = off;
+  const size_t lb_words    = size_t(max_tiles) * RADIX_DIGITS;
+  off += align_up(2 * 4 * lb_words, 256);
+  const size_t ktmp_off    = off;
+  if (need_tmp)
+  {
+    off += align_up(size_t(n) * kb, 256);
+  }
+  const size_t vtmp_off = off;
+  if (need_tmp && has_vals)
+  {
+    off += align_up(size_t(n) * vb, 256);
+  }
+  const size_t total = std::max<size_t>(off, 1);
+
+  if (c.d_temp_storage == nullptr)
+  {
+    *c.temp_storage_bytes = total;
+    return;
+  }
+  if (n == 0 || nseg == 0)
+  {
+    return;
+  }
+  if (*c.temp_storage_bytes < total)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "temp storage is smaller than the size query returned");
+  }
+  if ((reinterpret_cast<uintptr_t>(c.d_temp_storage) & 255) != 0)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "temp storage is not 256-byte aligned");
+  }
+  for (int i = 0; i < 2; ++i)
+  {
+    if (c.keys[i] == nullptr || (reinterpret_cast<uintptr_t>(c.keys[i]) % kb) != 0
+        || (has_vals && (c.values[i] == nullptr || (reinterpret_cast<uintptr_t>(c.values[i]) % vb) != 0)))
+    {
+      throw cuda_error(CUDA_ERROR_INVALID_VALUE, "key/value buffers must be non-null and element aligned");
+    }
+  }
+  if (c.begin_offsets == nullptr || c.end_offsets == nullptr)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "segment offsets are null");
+  }
+
+  auto* base     = static_cast<unsigned char*>(c.d_temp_storage);
+  auto* counters = reinterpret_cast<uint32_t*>(base + ctrl_off);
+  uint32_t* status = counters + (SEG_COUNTERS - 1);
+  auto* lists    = reinterpret_cast<uint32_t*>(base + lists_off);
+  const size_t list_stride = align_up(4 * size_t(nseg), 256) / 4;
+  auto* dev_list = reinterpret_cast<DeviceSegment*>(base + dev_off);
+  auto* tseg     = reinterpret_cast<uint32_t*>(base + tseg_off);
+  auto* counts   = reinterpret_cast<uint32_t*>(base + counts_off);
+  auto* bins     = reinterpret_cast<unsigned long long*>(base + bins_off);
+  uint32_t* lb[2] = {reinterpret_cast<uint32_t*>(base + lb_off), reinterpret_cast<uint32_t*>(base + lb_off) + lb_words};
+  void* ktmp     = base + ktmp_off;
+  void* vtmp     = base + vtmp_off;
+
+  const KeyCodec codec = make_codec(pol.key_kind, kb, c.descending);
+  const int sms        = sm_count();
+  void* final_keys     = c.keys[target];
+  void* final_vals     = has_vals ? c.values[target] : nullptr;
+
+  // 1. zero the counters and the per-segment digit counts
+  {
+    InitParams p{};
+    p.words     = counters;
+    p.num_words = zero_bytes / 4;
+    launch("seg_init", ks.k[SK_INIT], unsigned(std::min<uint64_t>(ceil_div(p.num_words, 256), 4096)), 256, 0, c.stream,
+           p);
+  }
+  // 2. size classes, on the device
+  {
+    SegClassifyParams p{};
+    p.begin_offsets   = c.begin_offsets;
+    p.end_offsets     = c.end_offsets;
+    p.offsets_64      = c.offsets_64;
+    p.partition       = nseg > uint64_t(SEG_PARTITION_THRESHOLD);
+    p.num_segments    = nseg;
+    p.num_items       = n;
+    p.max_device_segments = max_dev;
+    p.max_tiles       = max_tiles;
+    p.small_tile      = pol.small_threads * pol.small_items;
+    p.medium_tile     = pol.medium_threads * pol.medium_items;
+    p.block_small_cap = pol.block_s_cap;
+    p.block_large_cap = pol.block_l_cap;
+    p.device_tile     = uint32_t(pass_tile);
+    p.counters        = counters;
+    p.small_list      = lists;
+    p.medium_list     = lists + list_stride;
+    p.block_s_list    = lists + 2 * list_stride;
+    p.block_l_list    = lists + 3 * list_stride;
+    p.device_list     = dev_list;
+    p.tile_segment    = tseg;
+    p.status          = status;
+    launch("seg_classify", ks.k[SK_CLASSIFY], unsigned(std::min<uint64_t>(ceil_div(nseg, 256), uint64_t(sms) * 8)), 256,
+           0, c.stream, p);
+  }
+  // 3. warp and block classes: straight from the input into the final buffer
+  {
+    SegSortParams p{};
+    p.keys_in       = c.keys[0];
+    p.keys_out      = final_keys;
+    p.values_in     = has_vals ? c.values[0] : nullptr;
+    p.values_out    = final_vals;
+    p.begin_offsets = c.begin_offsets;
+    p.end_offsets   = c.end_offsets;
+    p.offsets_64    = c.offsets_64;
+    p.descending    = c.descending ? 1 : 0;
+    p.counters      = counters;
+    p.small_list    = lists;
+    p.medium_list   = lists + list_stride;
+    p.block_s_list  = lists + 2 * list_stride;
+    p.block_l_list  = lists + 3 * list_stride;
+    p.codec         = codec;
+    if (nseg > uint64_t(SEG_PARTITION_THRESHOLD))
+    {
+      launch("seg_small", ks.k[SK_SMALL], unsigned(sms * occupancy(ks.k[SK_SMALL], SEG_NETWORK_TPB, pol.network_small_smem)),
+             SEG_NETWORK_TPB, pol.network_small_smem, c.stream, p);
+    }
+    launch("seg_medium", ks.k[SK_MEDIUM],
+           unsigned(sms * occupancy(ks.k[SK_MEDIUM], SEG_NETWORK_TPB, pol.network_medium_smem)), SEG_NETWORK_TPB,
+           pol.network_medium_smem, c.stream, p);
+    launch("seg_block_s", ks.k[SK_BLOCK_S], unsigned(sms * occupancy(ks.k[SK_BLOCK_S], SEG_BLOCK_S_TPB, pol.block_s_smem)),
+           SEG_BLOCK_S_TPB, pol.block_s_smem, c.stream, p);
+    launch("seg_block_l", ks.k[SK_BLOCK_L], unsigned(sms * occupancy(ks.k[SK_BLOCK_L], SEG_BLOCK_L_TPB, pol.block_l_smem)),
+           SEG_BLOCK_L_TPB, pol.block_l_smem, c.stream, p);
+  }
+  // 4. device class: every large segment together, one launch per digit pass
+  if (max_dev > 0)
+  {
+    SegDeviceParams p{};
+    p.keys_in     = c.keys[0];
+    p.num_items   = n;
+    p.num_passes  = passes;
+    p.device_tile = uint32_t(pass_tile);
+    p.counters    = counters;
+    p.device_list = dev_list;
+    p.tile_segment = tseg;
+    p.seg_counts  = counts;
+    p.seg_bins    = bins;
+    p.lookback[0] = lb[0];
+    p.lookback[1] = lb[1];
+    p.status      = status;
+    p.codec       = codec;
+    for (int q = 0; q < passes; ++q)
+    {
+      p.pass_bit[q]  = bit[q];
+      p.pass_bits[q] = bits[q];
+      void* kd;
+      void* vd;
+      if (c.overwrite)
+      {
+        kd = c.keys[(q + 1) & 1];
+        vd = has_vals ? c.values[(q + 1) & 1] : nullptr;
+      }
+      else
+      {
+        const bool to_out = ((passes - 1 - q) % 2) == 0;
+        kd                = to_out ? c.keys[1] : ktmp;
+        vd                = has_vals ? (to_out ? c.values[1] : vtmp) : nullptr;
+      }
+      p.keys_dst[q]   = kd;
+      p.values_dst[q] = vd;
+      p.keys_src[q]   = q == 0 ? c.keys[0] : p.keys_dst[q - 1];
+      p.values_src[q] = has_vals ? (q == 0 ? c.values[0] : p.values_dst[q - 1]) : nullptr;
+    }
+    launch("seg_hist", ks.k[SK_HIST], unsigned(sms * 4), HISTOGRAM_TPB, 0, c.stream, p);
+    launch("seg_scan", ks.k[SK_SCAN], unsigned(sms * 4), 256, 0, c.stream, p);
+    const unsigned pass_grid = unsigned(sms * occupancy(ks.k[SK_PASS], pol.pass_tpb, pol.pass_smem));
+    for (int q = 0; q < passes; ++q)
+    {
+      p.pass = q;
+      launch("seg_pass", ks.k[SK_PASS], pass_grid, unsigned(pol.pass_tpb), pol.pass_smem, c.stream, p);
+    }
+  }
+  *selector = target;
+}
+
+} // namespace gb300

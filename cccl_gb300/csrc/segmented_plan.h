@@ -1,0 +1,80 @@
+// Host dispatcher of the batched segmented sort: temporary-storage plan, digit-pass plan
+// that lands the result in the buffer CUB's DeviceSegmentedSort would use, and the launch
+// sequence init -> classify -> class kernels -> large-segment passes.
+#pragma once
+
+#include <cuda.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "sort_params.h"
+
+namespace gb300
+{
+
+struct SegmentedPolicy
+{
+  uint32_t magic;
+  int32_t key_bytes;
+  int32_t value_bytes;
+  int32_t key_kind;
+  int32_t small_threads;
+  int32_t small_items;
+  int32_t medium_threads;
+  int32_t medium_items;
+  int32_t block_s_cap;
+  int32_t block_l_cap;
+  int32_t pass_tpb;
+  int32_t pass_items;
+  uint64_t network_small_smem;
+  uint64_t network_medium_smem;
+  uint64_t block_s_smem;
+  uint64_t block_l_smem;
+  uint64_t pass_smem;
+};
+
+SegmentedPolicy make_segmented_policy(int key_bytes, int value_bytes, int key_kind);
+
+// Kernels resolved from the library (names in segmented_sort_abi.cpp).
+enum SegKernel : int
+{
+  SK_INIT = 0,
+  SK_CLASSIFY,
+  SK_SMALL,
+  SK_MEDIUM,
+  SK_BLOCK_S,
+  SK_BLOCK_L,
+  SK_HIST,
+  SK_SCAN,
+  SK_PASS,
+  SK_COUNT
+};
+
+struct SegmentedKernels
+{
+  CUkernel k[SK_COUNT];
+};
+
+struct SegmentedCall
+{
+  void* keys[2];   // [0] = current (input), [1] = alternate (output)
+  void* values[2]; // null for keys-only
+  uint64_t num_items;
+  uint64_t num_segments;
+  const void* begin_offsets;
+  const void* end_offsets;
+  int offsets_64;
+  bool overwrite;
+  bool descending;
+  void* d_temp_storage;
+  size_t* temp_storage_bytes;
+  CUstream stream;
+};
+
+// Runs (or sizes, when d_temp_storage is null) one segmented sort; writes the selector
+// CUB's dispatch leaves in the caller's DoubleBuffer. Throws cuda_error on failure.
+void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels& ks, const SegmentedCall& call,
+                             int* selector);
+
+} // namespace gb300

@@ -1,111 +1,503 @@
-// C ABI of the batched segmented sort (reference: c/parallel/include/cccl/c/segmented_sort.h).
-// Entry points are exported now; the run path is filled in with the segmented kernels.
+// C ABI of the batched segmented sort: cccl_device_segmented_sort_{build,build_ex,compile,
+// load,link_ltoir,serialize,deserialize,cleanup} and the run entry cccl_device_segmented_sort.
+//
+// Reference interface: c/parallel/include/cccl/c/segmented_sort.h:27-139, implemented in
+// c/parallel/src/segmented_sort.cu (run :859-985: null selector rejected :875-881, keys and
+// values must be pointers, offsets through iterators :916-917).
 #include <cccl/c/segmented_sort.h>
 
+#include <memory>
+
 #include "abi_common.h"
+#include "segmented_plan.h"
+#include "sort_policy.h"
 
 using namespace gb300;
+
+namespace
+{
+
+constexpr uint32_t SEG_POLICY_MAGIC = 0x53425047u; // "GPBS"
+constexpr uint32_t SEG_TABLE_MAGIC  = 0x54425047u; // "GPBT"
+constexpr uint32_t ALGO_SEGMENTED   = 8u;          // CCCL_SERIALIZATION_ALGO_SEGMENTED_SORT
+
+// Names (and, once loaded, handles) of every kernel the run needs; kept in the build
+// result's partition_runtime_policy slot, which the reference uses for its partition policy.
+struct SegKernelTable
+{
+  uint32_t magic;
+  char names[SK_COUNT][64];
+  CUkernel handles[SK_COUNT];
+};
+
+bool keys_only(const cccl_iterator_t& values)
+{
+  return values.type == CCCL_POINTER && values.state == nullptr;
+}
+
+const char* kind_suffix(int kind)
+{
+  return kind == KIND_FLOAT ? "f" : kind == KIND_SIGNED ? "i" : "u";
+}
+
+void set_name(SegKernelTable& t, int i, const std::string& s)
+{
+  std::snprintf(t.names[i], sizeof(t.names[i]), "%s", s.c_str());
+}
+
+void free_result(cccl_device_segmented_sort_build_result_t* b)
+{
+  delete[] static_cast<char*>(b->payload);
+  b->payload = nullptr;
+  std::free(b->runtime_policy);
+  b->runtime_policy = nullptr;
+  std::free(b->partition_runtime_policy);
+  b->partition_runtime_policy = nullptr;
+  for (char** p :
+       {&b->segmented_sort_fallback_kernel_lowered_name,
+        &b->segmented_sort_kernel_small_lowered_name,
+        &b->segmented_sort_kernel_large_lowered_name,
+        &b->three_way_partition_init_kernel_lowered_name,
+        &b->three_way_partition_kernel_lowered_name})
+  {
+    delete[] *p;
+    *p = nullptr;
+  }
+}
+
+} // namespace
 
 extern "C" {
 
 CCCL_C_API CUresult cccl_device_segmented_sort_compile(
-  cccl_device_segmented_sort_build_result_t*,
-  cccl_sort_order_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  int,
-  int,
+  cccl_device_segmented_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t begin_offset_in,
+  cccl_iterator_t /*end_offset_in*/,
+  int cc_major,
+  int cc_minor,
   const char*,
   const char*,
   const char*,
   const char*,
   cccl_build_config*)
+try
 {
-  return CUDA_ERROR_NOT_SUPPORTED;
+  if (build == nullptr || (sort_order != CCCL_ASCENDING && sort_order != CCCL_DESCENDING))
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (cc_major * 10 + cc_minor != 103)
+  {
+    printf("\nERROR in cccl_device_segmented_sort_compile(): kernels are built for sm_103a only (requested %d.%d)\n",
+           cc_major,
+           cc_minor);
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  int kind = 0, kb = 0;
+  if (!key_kind_of(d_keys_in.value_type.type, kind, kb) || d_keys_in.value_type.size != size_t(kb))
+  {
+    printf("\nERROR in cccl_device_segmented_sort_compile(): unsupported key type\n");
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  const size_t vb = keys_only(d_values_in) ? 0 : d_values_in.value_type.size;
+  if (!(vb == 0 || vb == 4 || vb == 8))
+  {
+    printf("\nERROR in cccl_device_segmented_sort_compile(): value size %zu is not supported (0, 4 or 8)\n", vb);
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  const image_ref img = segmented_image(kb);
+  std::unique_ptr<char[]> payload(new char[img.size]);
+  std::memcpy(payload.get(), img.data, img.size);
+
+  auto* pol = static_cast<SegmentedPolicy*>(std::malloc(sizeof(SegmentedPolicy)));
+  auto* tab = static_cast<SegKernelTable*>(std::calloc(1, sizeof(SegKernelTable)));
+  if (pol == nullptr || tab == nullptr)
+  {
+    std::free(pol);
+    std::free(tab);
+    return CUDA_ERROR_OUT_OF_MEMORY;
+  }
+  *pol       = make_segmented_policy(kb, int(vb), kind);
+  pol->magic = SEG_POLICY_MAGIC;
+  tab->magic = SEG_TABLE_MAGIC;
+  const std::string kv  = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_";
+  const std::string net = kv + kind_suffix(kind);
+  const std::string rad = kv + (kind == KIND_FLOAT ? "f" : "i");
+  set_name(*tab, SK_INIT, "gb300_init");
+  set_name(*tab, SK_CLASSIFY, "gb300_seg_classify");
+  set_name(*tab, SK_SMALL, "gb300_seg_small_" + net);
+  set_name(*tab, SK_MEDIUM, "gb300_seg_medium_" + net);
+  set_name(*tab, SK_BLOCK_S, "gb300_seg_block_s_" + rad);
+  set_name(*tab, SK_BLOCK_L, "gb300_seg_block_l_" + rad);
+  set_name(*tab, SK_HIST, "gb300_seg_hist_k" + std::to_string(kb) + (kind == KIND_FLOAT ? "_f" : "_i"));
+  set_name(*tab, SK_SCAN, "gb300_seg_scan");
+  set_name(*tab, SK_PASS, "gb300_seg_pass_" + rad);
+
+  cccl_device_segmented_sort_build_result_t r{};
+  r.cc                            = cc_major * 10 + cc_minor;
+  r.payload                       = payload.release();
+  r.payload_size                  = img.size;
+  r.payload_kind                  = CCCL_PAYLOAD_CUBIN;
+  r.key_type                      = d_keys_in.value_type;
+  r.offset_type                   = begin_offset_in.value_type;
+  r.runtime_policy                = pol;
+  r.runtime_policy_size           = sizeof(SegmentedPolicy);
+  r.partition_runtime_policy      = tab;
+  r.partition_runtime_policy_size = sizeof(SegKernelTable);
+  r.order                         = sort_order;
+  r.segmented_sort_fallback_kernel_lowered_name = dup_cstr(tab->names[SK_PASS]);
+  r.segmented_sort_kernel_small_lowered_name    = dup_cstr(tab->names[SK_SMALL]);
+  r.segmented_sort_kernel_large_lowered_name    = dup_cstr(tab->names[SK_BLOCK_L]);
+  r.three_way_partition_init_kernel_lowered_name = dup_cstr(tab->names[SK_INIT]);
+  r.three_way_partition_kernel_lowered_name      = dup_cstr(tab->names[SK_CLASSIFY]);
+  *build                                         = r;
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_segmented_sort_compile", e);
 }
 
-CCCL_C_API CUresult cccl_device_segmented_sort_load(cccl_device_segmented_sort_build_result_t*)
+CCCL_C_API CUresult cccl_device_segmented_sort_load(cccl_device_segmented_sort_build_result_t* build)
+try
 {
-  return CUDA_ERROR_NOT_SUPPORTED;
+  if (build == nullptr || build->payload == nullptr || build->payload_size == 0
+      || build->payload_kind != CCCL_PAYLOAD_CUBIN || build->partition_runtime_policy == nullptr
+      || build->partition_runtime_policy_size != sizeof(SegKernelTable)
+      || static_cast<SegKernelTable*>(build->partition_runtime_policy)->magic != SEG_TABLE_MAGIC)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  const CUresult st = cuLibraryLoadData(&build->library, build->payload, nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (st != CUDA_SUCCESS)
+  {
+    return st;
+  }
+  auto* tab = static_cast<SegKernelTable*>(build->partition_runtime_policy);
+  try
+  {
+    for (int i = 0; i < SK_COUNT; ++i)
+    {
+      check(cuLibraryGetKernel(&tab->handles[i], build->library, tab->names[i]), tab->names[i]);
+    }
+  }
+  catch (...)
+  {
+    cuLibraryUnload(build->library);
+    build->library = nullptr;
+    throw;
+  }
+  build->segmented_sort_fallback_kernel  = tab->handles[SK_PASS];
+  build->segmented_sort_kernel_small     = tab->handles[SK_SMALL];
+  build->segmented_sort_kernel_large     = tab->handles[SK_BLOCK_L];
+  build->three_way_partition_init_kernel = tab->handles[SK_INIT];
+  build->three_way_partition_kernel      = tab->handles[SK_CLASSIFY];
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_segmented_sort_load", e);
 }
 
 CCCL_C_API CUresult cccl_device_segmented_sort_build_ex(
-  cccl_device_segmented_sort_build_result_t*,
-  cccl_sort_order_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  int,
-  int,
-  const char*,
-  const char*,
-  const char*,
-  const char*,
-  cccl_build_config*)
+  cccl_device_segmented_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t begin_offset_in,
+  cccl_iterator_t end_offset_in,
+  int cc_major,
+  int cc_minor,
+  const char* cub_path,
+  const char* thrust_path,
+  const char* libcudacxx_path,
+  const char* ctk_path,
+  cccl_build_config* config)
 {
-  return CUDA_ERROR_NOT_SUPPORTED;
+  CUresult r = cccl_device_segmented_sort_compile(
+    build,
+    sort_order,
+    d_keys_in,
+    d_values_in,
+    begin_offset_in,
+    end_offset_in,
+    cc_major,
+    cc_minor,
+    cub_path,
+    thrust_path,
+    libcudacxx_path,
+    ctk_path,
+    config);
+  if (r != CUDA_SUCCESS)
+  {
+    return r;
+  }
+  r = cccl_device_segmented_sort_load(build);
+  if (r != CUDA_SUCCESS)
+  {
+    cccl_device_segmented_sort_cleanup(build);
+  }
+  return r;
 }
 
 CCCL_C_API CUresult cccl_device_segmented_sort_build(
-  cccl_device_segmented_sort_build_result_t*,
-  cccl_sort_order_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  int,
-  int,
-  const char*,
-  const char*,
-  const char*,
-  const char*)
+  cccl_device_segmented_sort_build_result_t* build,
+  cccl_sort_order_t sort_order,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t begin_offset_in,
+  cccl_iterator_t end_offset_in,
+  int cc_major,
+  int cc_minor,
+  const char* cub_path,
+  const char* thrust_path,
+  const char* libcudacxx_path,
+  const char* ctk_path)
 {
-  return CUDA_ERROR_NOT_SUPPORTED;
+  return cccl_device_segmented_sort_build_ex(
+    build,
+    sort_order,
+    d_keys_in,
+    d_values_in,
+    begin_offset_in,
+    end_offset_in,
+    cc_major,
+    cc_minor,
+    cub_path,
+    thrust_path,
+    libcudacxx_path,
+    ctk_path,
+    nullptr);
 }
 
 CCCL_C_API CUresult cccl_device_segmented_sort(
-  cccl_device_segmented_sort_build_result_t,
-  void*,
-  size_t*,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  uint64_t,
-  uint64_t,
-  cccl_iterator_t,
-  cccl_iterator_t,
-  bool,
-  int*,
-  CUstream)
+  cccl_device_segmented_sort_build_result_t build,
+  void* d_temp_storage,
+  size_t* temp_storage_bytes,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_keys_out,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t d_values_out,
+  uint64_t num_items,
+  uint64_t num_segments,
+  cccl_iterator_t start_offset_in,
+  cccl_iterator_t end_offset_in,
+  bool is_overwrite_okay,
+  int* selector,
+  CUstream stream)
 {
+  if (selector == nullptr)
+  {
+    fflush(stderr);
+    printf("\nERROR in cccl_device_segmented_sort(): selector cannot be nullptr\n");
+    fflush(stdout);
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (d_keys_in.type != CCCL_POINTER || d_keys_out.type != CCCL_POINTER || d_values_in.type != CCCL_POINTER
+      || d_values_out.type != CCCL_POINTER)
+  {
+    fflush(stderr);
+    printf("\nERROR in cccl_device_segmented_sort(): keys and values must be pointers\n");
+    fflush(stdout);
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (start_offset_in.type != CCCL_POINTER || end_offset_in.type != CCCL_POINTER)
+  {
+    printf("\nERROR in cccl_device_segmented_sort(): segment offsets must be pointers\n");
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  const size_t osz = start_offset_in.value_type.size;
+  if ((osz != 4 && osz != 8) || end_offset_in.value_type.size != osz || temp_storage_bytes == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  try
+  {
+    context_guard ctx;
+    if (build.runtime_policy == nullptr || build.runtime_policy_size != sizeof(SegmentedPolicy)
+        || static_cast<const SegmentedPolicy*>(build.runtime_policy)->magic != SEG_POLICY_MAGIC
+        || build.partition_runtime_policy == nullptr || build.library == nullptr)
+    {
+      return CUDA_ERROR_NOT_INITIALIZED;
+    }
+    const auto& pol = *static_cast<const SegmentedPolicy*>(build.runtime_policy);
+    const auto& tab = *static_cast<const SegKernelTable*>(build.partition_runtime_policy);
+    SegmentedKernels ks{};
+    for (int i = 0; i < SK_COUNT; ++i)
+    {
+      ks.k[i] = tab.handles[i];
+    }
+    SegmentedCall call{};
+    call.keys[0]            = d_keys_in.state;
+    call.keys[1]            = d_keys_out.state;
+    call.values[0]          = d_values_in.state;
+    call.values[1]          = d_values_out.state;
+    call.num_items          = num_items;
+    call.num_segments       = num_segments;
+    call.begin_offsets      = start_offset_in.state;
+    call.end_offsets        = end_offset_in.state;
+    call.offsets_64         = osz == 8 ? 1 : 0;
+    call.overwrite          = is_overwrite_okay;
+    call.descending         = build.order == CCCL_DESCENDING;
+    call.d_temp_storage     = d_temp_storage;
+    call.temp_storage_bytes = temp_storage_bytes;
+    call.stream             = stream;
+    int sel                 = 0;
+    segmented_sort_dispatch(pol, ks, call, &sel);
+    *selector = sel;
+    return CUDA_SUCCESS;
+  }
+  catch (const std::exception& e)
+  {
+    return report("cccl_device_segmented_sort", e);
+  }
+}
+
+CCCL_C_API CUresult cccl_device_segmented_sort_link_ltoir(
+  cccl_device_segmented_sort_build_result_t* build, const void**, const size_t*, size_t)
+{
+  // The payload is a finished cubin: there is no LTO-IR stage to link into.
+  if (build == nullptr || build->payload == nullptr || build->payload_size == 0
+      || build->payload_kind != CCCL_PAYLOAD_LTOIR)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
   return CUDA_ERROR_NOT_SUPPORTED;
 }
 
-CCCL_C_API CUresult
-cccl_device_segmented_sort_link_ltoir(cccl_device_segmented_sort_build_result_t*, const void**, const size_t*, size_t)
+CCCL_C_API CUresult cccl_device_segmented_sort_serialize(
+  const cccl_device_segmented_sort_build_result_t* b, void** out_buf, size_t* out_size)
+try
 {
-  return CUDA_ERROR_NOT_SUPPORTED;
-}
-
-CCCL_C_API CUresult
-cccl_device_segmented_sort_serialize(const cccl_device_segmented_sort_build_result_t*, void**, size_t*)
-{
-  return CUDA_ERROR_NOT_SUPPORTED;
-}
-
-CCCL_C_API CUresult
-cccl_device_segmented_sort_deserialize(cccl_device_segmented_sort_build_result_t*, const void*, size_t)
-{
-  return CUDA_ERROR_NOT_SUPPORTED;
-}
-
-CCCL_C_API CUresult cccl_device_segmented_sort_cleanup(cccl_device_segmented_sort_build_result_t*)
-{
+  if (b == nullptr || out_buf == nullptr || out_size == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (b->payload == nullptr || b->payload_size == 0 || b->runtime_policy == nullptr
+      || b->partition_runtime_policy == nullptr)
+  {
+    *out_buf  = nullptr;
+    *out_size = 0;
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  SegKernelTable tab = *static_cast<const SegKernelTable*>(b->partition_runtime_policy);
+  for (auto& h : tab.handles)
+  {
+    h = nullptr; // handles belong to a loaded library; never serialized
+  }
+  blob_writer w;
+  write_header(w, ALGO_SEGMENTED, b->payload_kind, b->cc);
+  w.type_info(b->key_type);
+  w.type_info(b->offset_type);
+  w.pod<uint32_t>(uint32_t(b->order));
+  w.blob(b->payload, b->payload_size);
+  w.blob(b->runtime_policy, b->runtime_policy_size);
+  w.blob(&tab, sizeof(tab));
+  w.cstr(b->segmented_sort_fallback_kernel_lowered_name);
+  w.cstr(b->segmented_sort_kernel_small_lowered_name);
+  w.cstr(b->segmented_sort_kernel_large_lowered_name);
+  w.cstr(b->three_way_partition_init_kernel_lowered_name);
+  w.cstr(b->three_way_partition_kernel_lowered_name);
+  w.release(out_buf, out_size);
   return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_segmented_sort_serialize", e);
+}
+
+CCCL_C_API CUresult
+cccl_device_segmented_sort_deserialize(cccl_device_segmented_sort_build_result_t* build, const void* buf, size_t size)
+try
+{
+  if (build == nullptr || buf == nullptr || size == 0)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  blob_reader rd{static_cast<const unsigned char*>(buf), size};
+  const blob_header h = read_header(rd, ALGO_SEGMENTED);
+  cccl_device_segmented_sort_build_result_t r{};
+  r.cc           = h.cc;
+  r.payload_kind = cccl_payload_kind_t(h.payload_kind);
+  r.key_type     = rd.type_info();
+  r.offset_type  = rd.type_info();
+  r.order        = cccl_sort_order_t(rd.pod<uint32_t>());
+  if (r.order != CCCL_ASCENDING && r.order != CCCL_DESCENDING)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: invalid sort order");
+  }
+  std::unique_ptr<char[]> payload(static_cast<char*>(rd.blob_new(&r.payload_size)));
+  size_t pol_size = 0, tab_size = 0;
+  std::unique_ptr<char[]> pol_bytes(static_cast<char*>(rd.blob_new(&pol_size)));
+  std::unique_ptr<char[]> tab_bytes(static_cast<char*>(rd.blob_new(&tab_size)));
+  if (r.payload_size == 0 || pol_size != sizeof(SegmentedPolicy) || tab_size != sizeof(SegKernelTable))
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: size mismatch");
+  }
+  auto* pol = static_cast<SegmentedPolicy*>(std::malloc(sizeof(SegmentedPolicy)));
+  auto* tab = static_cast<SegKernelTable*>(std::malloc(sizeof(SegKernelTable)));
+  if (pol == nullptr || tab == nullptr)
+  {
+    std::free(pol);
+    std::free(tab);
+    return CUDA_ERROR_OUT_OF_MEMORY;
+  }
+  std::memcpy(pol, pol_bytes.get(), sizeof(SegmentedPolicy));
+  std::memcpy(tab, tab_bytes.get(), sizeof(SegKernelTable));
+  if (pol->magic != SEG_POLICY_MAGIC || tab->magic != SEG_TABLE_MAGIC)
+  {
+    std::free(pol);
+    std::free(tab);
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: bad policy");
+  }
+  for (auto& name : tab->names)
+  {
+    name[sizeof(name) - 1] = '\0';
+  }
+  std::unique_ptr<char[]> names[5];
+  for (auto& n : names)
+  {
+    n.reset(rd.cstr_new());
+  }
+  r.payload                                      = payload.release();
+  r.runtime_policy                               = pol;
+  r.runtime_policy_size                          = sizeof(SegmentedPolicy);
+  r.partition_runtime_policy                     = tab;
+  r.partition_runtime_policy_size                = sizeof(SegKernelTable);
+  r.segmented_sort_fallback_kernel_lowered_name  = names[0].release();
+  r.segmented_sort_kernel_small_lowered_name     = names[1].release();
+  r.segmented_sort_kernel_large_lowered_name     = names[2].release();
+  r.three_way_partition_init_kernel_lowered_name = names[3].release();
+  r.three_way_partition_kernel_lowered_name      = names[4].release();
+  *build                                         = r;
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_segmented_sort_deserialize", e);
+}
+
+CCCL_C_API CUresult cccl_device_segmented_sort_cleanup(cccl_device_segmented_sort_build_result_t* b)
+try
+{
+  if (b == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  free_result(b);
+  if (b->library != nullptr)
+  {
+    check(cuLibraryUnload(b->library), "cuLibraryUnload");
+    b->library = nullptr;
+  }
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_device_segmented_sort_cleanup", e);
 }
 
 } // extern "C"

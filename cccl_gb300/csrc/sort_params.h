@@ -16,7 +16,8 @@ constexpr int LOOKBACK_BATCH = 8; // predecessor rows read per look-back step
 
 // Status word bits reported by the kernels (OR-ed into SortControl::status).
 constexpr uint32_t STATUS_LOOKBACK_TIMEOUT = 1u;
-constexpr uint32_t STATUS_BAD_SEGMENT      = 2u;
+constexpr uint32_t STATUS_BAD_SEGMENT      = 2u; // a segment outside the keys (left unsorted)
+constexpr uint32_t STATUS_SEG_CAPACITY     = 4u; // overlapping segments exceeded the plan: large ones skipped
 
 // Bit-order codec. encoded = raw ^ (raw & H ? fwd_neg : fwd_pos);
 // raw = encoded ^ (encoded & H ? inv_set : inv_clr). Only the low key-width bits are used.
@@ -94,6 +95,84 @@ struct SingleTileParams
   int begin_bit;
   int end_bit;
   int pad0;
+  KeyCodec codec;
+};
+
+// ---- batched segmented sort ----
+constexpr int SEG_MAX_PASSES = 12; // 8-bit digits, plus one split pass to match CUB's buffer parity
+
+struct DeviceSegment
+{
+  unsigned long long begin;
+  uint32_t size;
+  uint32_t tile_base;
+};
+
+struct SegClassifyParams
+{
+  const void* begin_offsets;
+  const void* end_offsets;
+  int offsets_64;
+  int partition; // more than 500 segments: small segments get their own network
+  unsigned long long num_segments;
+  unsigned long long num_items;           // segments reaching past it are rejected
+  unsigned long long max_device_segments; // capacity of device_list (temp-storage plan)
+  unsigned long long max_tiles;           // capacity of tile_segment
+  long long small_tile;
+  long long medium_tile;
+  long long block_small_cap;
+  long long block_large_cap;
+  uint32_t device_tile;
+  uint32_t pad0;
+  uint32_t* counters;
+  uint32_t* small_list;
+  uint32_t* medium_list;
+  uint32_t* block_s_list;
+  uint32_t* block_l_list;
+  DeviceSegment* device_list;
+  uint32_t* tile_segment;
+  uint32_t* status;
+};
+
+struct SegSortParams
+{
+  const void* keys_in;
+  void* keys_out; // final buffer (may alias keys_in)
+  const void* values_in;
+  void* values_out;
+  const void* begin_offsets;
+  const void* end_offsets;
+  int offsets_64;
+  int descending;
+  uint32_t* counters;
+  const uint32_t* small_list;
+  const uint32_t* medium_list;
+  const uint32_t* block_s_list;
+  const uint32_t* block_l_list;
+  KeyCodec codec;
+};
+
+struct SegDeviceParams
+{
+  const void* keys_in; // original keys (histogram)
+  const void* keys_src[SEG_MAX_PASSES];
+  void* keys_dst[SEG_MAX_PASSES];
+  const void* values_src[SEG_MAX_PASSES];
+  void* values_dst[SEG_MAX_PASSES];
+  unsigned long long num_items;
+  int num_passes;
+  int pass; // the pass a pass-kernel launch performs
+  int pass_bit[SEG_MAX_PASSES];
+  int pass_bits[SEG_MAX_PASSES];
+  uint32_t device_tile;
+  uint32_t pad0;
+  uint32_t* counters;
+  const DeviceSegment* device_list;
+  const uint32_t* tile_segment;
+  uint32_t* seg_counts;
+  unsigned long long* seg_bins;
+  uint32_t* lookback[2];
+  uint32_t* status;
   KeyCodec codec;
 };
 

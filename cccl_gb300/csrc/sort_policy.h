@@ -137,3 +137,57 @@ static_assert(persistent_smem_bytes(8, 8) * PERSISTENT_MINB <= 227 * 1024
               "persistent tile buffers exceed shared memory");
 
 } // namespace gb300
+
+// ---- batched segmented sort: size classes ----
+namespace gb300
+{
+// CUB's sub-warp network shapes for cc >= 8.6 (tuning_segmented_sort.cuh:182-195, items
+// scaled as cub/cub/util_math.cuh:54-57). They fix the bit-exact NaN placement, so they
+// are not tuning knobs here.
+GB300_HD constexpr int seg_scale_items(int nominal, int dominant)
+{
+  return (nominal * 4 / dominant) < 1 ? 1 : (nominal * 4 / dominant) > nominal ? nominal : (nominal * 4 / dominant);
+}
+GB300_HD constexpr int seg_dominant(int kb, int vb)
+{
+  return kb > vb ? kb : vb;
+}
+GB300_HD constexpr int seg_small_threads(int kb, int vb)
+{
+  return seg_dominant(kb, vb) > 4 ? 8 : 2;
+}
+GB300_HD constexpr int seg_small_items(int kb, int vb)
+{
+  return seg_scale_items(seg_dominant(kb, vb) > 4 ? 7 : 9, seg_dominant(kb, vb));
+}
+GB300_HD constexpr int seg_medium_threads(int, int)
+{
+  return 16;
+}
+GB300_HD constexpr int seg_medium_items(int kb, int vb)
+{
+  return seg_scale_items(seg_dominant(kb, vb) > 4 ? 9 : 7, seg_dominant(kb, vb));
+}
+constexpr int SEG_PARTITION_THRESHOLD = 500; // dispatch_segmented_sort.cuh:465
+
+// Block classes (tuned here, free of the reference): one CTA, shared-memory passes.
+constexpr int SEG_BLOCK_S_TPB   = 256;
+constexpr int SEG_BLOCK_S_ITEMS = 8;  // <= 2048 keys
+constexpr int SEG_BLOCK_L_TPB   = 512;
+constexpr int SEG_BLOCK_L_ITEMS = 16; // <= 8192 keys
+constexpr int SEG_NETWORK_TPB   = 256;
+constexpr int SEG_PASS_TPB      = ONESWEEP_TPB;
+} // namespace gb300
+
+namespace gb300
+{
+GB300_HD constexpr size_t seg_network_smem(int kb, int vb, int threads, int items)
+{
+  return size_t(SEG_NETWORK_TPB / 32) * size_t(32 / threads)
+       * (round16(size_t(kb) * (threads * items + 1)) + (vb > 0 ? round16(value_word_bytes(vb) * (threads * items + 1)) : 0));
+}
+GB300_HD constexpr size_t block_sort_smem(int kb, int tpb, int items)
+{
+  return size_t(4) * (tpb / 32) * 256 + 128 + round16(size_t(2) * kb * tpb * items) + size_t(2) * 2 * tpb * items;
+}
+} // namespace gb300

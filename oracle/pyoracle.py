@@ -95,12 +95,12 @@ def radix_permutation(keys, begin_bit=0, end_bit=None, descending=False, threads
 def segmented_sort(keys, values, begin_offsets, end_offsets, descending=False, threads=1):
     """cub::DeviceSegmentedSort result (size classes and merge network included)."""
     keys = np.ascontiguousarray(keys)
-    ko = np.empty_like(keys)
+    ko = keys.copy()  # positions outside every segment keep the input (the sort does not write them)
     vo = None
     vb = 0
     if values is not None:
         values = np.ascontiguousarray(values)
-        vo = np.empty_like(values)
+        vo = values.copy()
         vb = values.dtype.itemsize
     b = np.ascontiguousarray(begin_offsets, dtype=np.int64)
     e = np.ascontiguousarray(end_offsets, dtype=np.int64)

@@ -89,3 +89,40 @@ def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, ove
     if return_temp:
         return kres, vres, sel, temp
     return kres, vres, sel
+
+
+def gpu_seg_sort(keys, values, begin, end, descending=False, overwrite=False, offsets_dtype=np.int32):
+    """Sorts segments through cccl_device_segmented_sort. Output buffers start as copies of
+    the input so positions outside every segment compare equal. Returns (keys, values, selector)."""
+    import torch
+
+    from cccl_gb300 import DoubleBuffer, SortOrder, make_segmented_sort
+
+    order = SortOrder.DESCENDING if descending else SortOrder.ASCENDING
+    ki = to_dev(keys)
+    ko = to_dev(keys)
+    vi = vo = None
+    if values is not None:
+        vi = value_tensor(values)
+        vo = value_tensor(values)
+    bo = torch.from_numpy(np.ascontiguousarray(begin, dtype=offsets_dtype)).cuda()
+    eo = torch.from_numpy(np.ascontiguousarray(end, dtype=offsets_dtype)).cuda()
+    if overwrite:
+        dk = DoubleBuffer(ki, ko)
+        dv = DoubleBuffer(vi, vo) if vi is not None else None
+        args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
+    else:
+        args = dict(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo)
+    s = make_segmented_sort(order=order, start_offsets_in=bo, end_offsets_in=eo, **args)
+    call = dict(num_items=keys.size, num_segments=len(begin), start_offsets_in=bo, end_offsets_in=eo, **args)
+    nbytes = s(temp_storage=None, **call)
+    temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
+    s(temp_storage=temp, **call)
+    torch.cuda.synchronize()
+    if overwrite:
+        sel = dk.selector
+        kout, vout = dk.current(), (dv.current() if dv is not None else None)
+    else:
+        sel = None
+        kout, vout = ko, vo
+    return from_dev(kout, keys.dtype), (from_dev(vout, values.dtype) if values is not None else None), sel

@@ -1,0 +1,120 @@
+"""Parity of the batched segmented sort (through cccl_device_segmented_sort) with the
+oracle's restatement of cub::DeviceSegmentedSort, bit for bit: size classes, the sub-warp
+merge network's NaN placement, +-0, empty and uncovered segments, both orders, DoubleBuffer
+selectors, int32/int64 offsets."""
+
+import numpy as np
+import pytest
+
+import inputs as I
+from segments import edge_segments, lognormal_segments
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_library):
+    import torch
+
+    assert torch.cuda.is_available()
+    return built_library
+
+
+def _check(oracle, keys, values, b, e, desc=False, overwrite=False, offsets_dtype=np.int32):
+    from gpu_util import gpu_seg_sort
+
+    ko, vo, sel = gpu_seg_sort(keys, values, b, e, desc, overwrite, offsets_dtype)
+    rk, rv = oracle.segmented_sort(keys, values, b, e, descending=desc, threads=8)
+    bad = np.nonzero(ko.view(np.uint8).reshape(keys.size, -1).any(1) != rk.view(np.uint8).reshape(keys.size, -1).any(1))
+    assert ko.tobytes() == rk.tobytes(), "keys differ from the oracle"
+    if values is not None:
+        assert vo.tobytes() == rv.tobytes(), "values differ from the oracle"
+    return sel
+
+
+def _nan_keys(dtype, n, rng, density=1 / 8):
+    return I.with_specials(I.finite_floats(dtype, n, rng), rng, density)
+
+
+EDGE_SIZES = [1, 2, 3, 4, 17, 18, 19, 20, 111, 112, 113, 200, 2047, 2048, 2049, 8191, 8192, 8193, 20000, 100_000]
+
+
+@pytest.mark.parametrize("many", [False, True], ids=["fallback", "partitioned"])
+@pytest.mark.parametrize("desc", [False, True])
+def test_size_class_edges_with_nans(oracle, many, desc):
+    rng = np.random.default_rng(7 + many + 2 * desc)
+    sizes = EDGE_SIZES * (30 if many else 1)  # > 500 segments switches on partitioning
+    b, e, n = edge_segments(sizes, gap=0)
+    k = _nan_keys(np.float32, n, rng)
+    v = I.index_values(n)
+    _check(oracle, k, v, b, e, desc)
+
+
+@pytest.mark.parametrize("desc", [False, True])
+@pytest.mark.parametrize("npairs", [False, True])
+def test_lognormal_batch_f32(oracle, desc, npairs):
+    """The batched configuration at 2^22 keys: lognormal(5, 2.5) lengths, 5% empty,
+    N(0,1) keys with 0.1% +-0 and NaN."""
+    rng = np.random.default_rng(2025 + desc)
+    b, e = lognormal_segments(rng, 1 << 22)
+    n = int(e[-1])
+    k = I.with_specials(rng.standard_normal(n).astype(np.float32), rng, 1e-3)
+    v = rng.integers(-(2**31), 2**31 - 1, size=n, dtype=np.int32) if npairs else None
+    _check(oracle, k, v, b, e, desc)
+
+
+@pytest.mark.parametrize(
+    "dtype,vdtype", [(np.int32, np.uint32), (np.uint64, np.uint64), (np.float64, np.int64), (np.float16, np.uint32),
+                     (np.uint8, None), (np.int16, np.uint32), (np.int64, None), (np.float32, None)]
+)
+def test_key_types(oracle, dtype, vdtype):
+    rng = np.random.default_rng(np.dtype(dtype).itemsize * 11 + (vdtype is None))
+    b, e = lognormal_segments(rng, 600_000, mu=4.0, sigma=2.0)
+    n = int(e[-1])
+    k = _nan_keys(dtype, n, rng, 1 / 64) if np.dtype(dtype).kind == "f" else I.entropy_reduced(dtype, n, rng, 2)
+    v = None if vdtype is None else I.uniform_bits(vdtype, n, rng)
+    for desc in (False, True):
+        _check(oracle, k, v, b, e, desc)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.uint64, np.uint8, np.float16])
+def test_overwrite_selector_matches_cub(oracle, dtype):
+    """With a DoubleBuffer the result lands where CUB's 6-bit (4-bit for 1-byte keys) radix
+    pass count puts it: selector = passes & 1 (dispatch_segmented_sort.cuh:730-739)."""
+    rng = np.random.default_rng(3)
+    b, e, n = edge_segments([5, 100, 3000, 9000, 70000, 1], gap=3)
+    k = _nan_keys(dtype, n, rng) if np.dtype(dtype).kind == "f" else I.uniform_bits(dtype, n, rng)
+    v = I.index_values(n)
+    kb = np.dtype(dtype).itemsize
+    expect = (-(-8 * kb // (6 if kb > 1 else 4))) & 1
+    sel = _check(oracle, k, v, b, e, overwrite=True)
+    assert sel == expect
+
+
+def test_empty_reversed_and_uncovered_segments(oracle):
+    rng = np.random.default_rng(9)
+    n = 50_000
+    k = _nan_keys(np.float32, n, rng)
+    v = I.index_values(n)
+    b = np.array([0, 10, 10, 500, 400, 20000, 45000], dtype=np.int64)
+    e = np.array([5, 10, 300, 499, 300, 44000, 50000], dtype=np.int64)  # empty, reversed (empty), gaps
+    _check(oracle, k, v, b, e, offsets_dtype=np.int64)
+    _check(oracle, k, v, b, e, desc=True, offsets_dtype=np.int32)
+
+
+def test_few_huge_segments(oracle):
+    """Device class: segments of millions of keys share the batched onesweep passes."""
+    rng = np.random.default_rng(11)
+    b, e, n = edge_segments([3_000_000, 1_500_001, 40_000, 2_000_000], gap=7)
+    k = I.with_specials(rng.standard_normal(n).astype(np.float32), rng, 1e-3)
+    v = I.index_values(n)
+    _check(oracle, k, v, b, e)
+    _check(oracle, k, v, b, e, desc=True, overwrite=True)
+
+
+def test_no_segments_and_no_items():
+    from gpu_util import gpu_seg_sort
+
+    k = np.arange(10, dtype=np.float32)
+    ko, _, _ = gpu_seg_sort(k, None, np.array([], dtype=np.int64), np.array([], dtype=np.int64))
+    assert ko.tobytes() == k.tobytes()
