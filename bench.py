@@ -203,6 +203,130 @@ def kernel_times(torch, sorter, steps):
     return {r: statistics.mean(v) for r, v in out.items()}, launches_per_step
 
 
+def segmented_workload(seed=77, total=1 << 27):
+    """BASELINE's batched configuration: f32 N(0,1) keys, 0.1% set to +-0.0/NaN, i32 values,
+    lognormal(5, 2.5) segment lengths clipped to [1, 2^23], 5% empty, int32 offsets."""
+    import numpy as np
+
+    import inputs as I
+    from segments import lognormal_segments
+
+    rng = np.random.default_rng(seed)
+    b, e = lognormal_segments(rng, total)
+    n = int(e[-1])
+    k = I.with_specials(rng.standard_normal(n).astype(np.float32), rng, 1e-3)
+    v = rng.integers(-(2**31), 2**31 - 1, size=n, dtype=np.int32)
+    return k, v, b.astype(np.int32), e.astype(np.int32)
+
+
+def run_segmented(torch, steps, per_segment_sample=4000):
+    """Batched segmented sort vs one plain radix-sort launch per segment (same GPU)."""
+    import numpy as np
+
+    from cccl_gb300 import SortOrder, make_radix_sort, make_segmented_sort
+
+    k, v, b, e = segmented_workload()
+    n, nseg = k.size, b.size
+    kd = torch.from_numpy(k).cuda()
+    vd = torch.from_numpy(v).cuda()
+    ko, vo = kd.clone(), vd.clone()
+    bo, eo = torch.from_numpy(b).cuda(), torch.from_numpy(e).cuda()
+    args = dict(d_in_keys=kd, d_out_keys=ko, d_in_values=vd, d_out_values=vo)
+    s = make_segmented_sort(order=SortOrder.ASCENDING, start_offsets_in=bo, end_offsets_in=eo, **args)
+    call = dict(num_items=n, num_segments=nseg, start_offsets_in=bo, end_offsets_in=eo, **args)
+    temp = torch.empty(s(temp_storage=None, **call), dtype=torch.uint8, device="cuda")
+
+    def once():
+        s(temp_storage=temp, **call)
+
+    ms = time_steps(torch, once, steps, 3, lambda: None)
+    # the same call sequence captured once in a CUDA graph and replayed
+    graph_ms = None
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            once()
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            once()
+        graph_ms = time_steps(torch, g.replay, steps, 2, lambda: None)
+    except Exception as exc:  # graph capture unavailable: report the plain number only
+        graph_ms = None
+        print(f"graph capture failed: {exc}", file=sys.stderr)
+    kt, launches = kernel_times_fn(torch, once)
+
+    # one plain radix SortPairs launch per segment, on a sample of the segments
+    sizes = e - b
+    idx = np.nonzero(sizes > 0)[0]
+    sample = idx[:: max(1, idx.size // per_segment_sample)]
+    rs = make_radix_sort(d_in_keys=kd, d_out_keys=ko, d_in_values=vd, d_out_values=vo, order=SortOrder.ASCENDING)
+    max_seg = int(sizes.max())
+    tb = max(rs(temp_storage=None, d_in_keys=kd[:max_seg], d_out_keys=ko[:max_seg], d_in_values=vd[:max_seg],
+                d_out_values=vo[:max_seg], num_items=max_seg), 1)
+    rtemp = torch.empty(tb, dtype=torch.uint8, device="cuda")
+    views = [(kd[b[i]:e[i]], ko[b[i]:e[i]], vd[b[i]:e[i]], vo[b[i]:e[i]], int(sizes[i])) for i in sample]
+
+    def per_segment():
+        for ki, kout, vi, vout, m in views:
+            rs(temp_storage=rtemp, d_in_keys=ki, d_out_keys=kout, d_in_values=vi, d_out_values=vout, num_items=m)
+
+    ps_ms = time_steps(torch, per_segment, 1, 1, lambda: None)
+    sample_items = int(sizes[sample].sum())
+    # scale the sample to the whole batch by its share of segments (launch-bound) and keys
+    ps_full_ms = ps_ms * max(idx.size / sample.size, 1.0)
+    peak, _ = _peaks()
+    alg_bytes = 4 * n * 2 * 8
+    return {
+        "workload": f"segmented SortPairs: 2^27 f32 keys (0.1% +-0/NaN) + i32 values, {nseg} lognormal(5,2.5) segments",
+        "num_items": n,
+        "num_segments": int(nseg),
+        "ms": ms,
+        "keys_per_s": n / (ms / 1e3),
+        "graph_ms": graph_ms,
+        "graph_keys_per_s": (n / (graph_ms / 1e3)) if graph_ms else None,
+        "roofline_frac_radix_equivalent": alg_bytes / (ms / 1e3) / 1e9 / peak,
+        "roofline_frac_one_pass_floor": (n * 16) / (ms / 1e3) / 1e9 / peak,
+        "kernel_ms": kt,
+        "launches_per_call": launches,
+        "per_segment_launch_ms_sample": ps_ms,
+        "per_segment_sample": {"segments": int(sample.size), "keys": sample_items},
+        "per_segment_launch_ms_estimated_full": ps_full_ms,
+        "speedup_vs_per_segment_launches": ps_full_ms / ms,
+    }
+
+
+def kernel_times_fn(torch, fn, steps=3):
+    from cccl_gb300 import _bindings as B
+
+    lib = B.load_library()
+    stream = torch.cuda.current_stream()
+    records = []
+
+    def observer(user, role, phase, s):
+        ev = torch.cuda.Event(enable_timing=True)
+        ev.record(stream)
+        records.append((role.decode(), phase, ev))
+
+    cb = B.LAUNCH_OBSERVER(observer)
+    lib.cccl_gb300_set_launch_observer(cb, None)
+    try:
+        for _ in range(steps):
+            fn()
+        torch.cuda.synchronize()
+    finally:
+        lib.cccl_gb300_set_launch_observer(B.LAUNCH_OBSERVER(0), None)
+    out, open_ev, count = {}, {}, 0
+    for role, phase, ev in records:
+        if phase == 0:
+            open_ev[role] = ev
+        else:
+            out[role] = out.get(role, 0.0) + open_ev.pop(role).elapsed_time(ev) / steps
+            count += 1
+    return out, count // steps
+
+
 def cpu_reference_sort(n_sample, threads, key_dtype="u64", with_values=True, reps=3):
     """thrust::sort_by_key on the OpenMP backend over a bounded sample (keys/s)."""
     import numpy as np
@@ -340,6 +464,12 @@ def run_engine(args):
     e2e_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
     torch.cuda.synchronize()
 
+    # the batched segmented configuration
+    segmented = None
+    if not args.no_variants:
+        segmented = run_segmented(torch, max(3, args.steps // 2))
+        torch.cuda.empty_cache()
+
     # variants of the configuration and the keys-only roofline row
     variants = []
     if not args.no_variants:
@@ -414,6 +544,7 @@ def run_engine(args):
                 "ms_per_step": e2e_ms},
         "cpu_baseline": cpu,
         "variants": variants,
+        "segmented": segmented,
     }
     print(json.dumps(line))
 

@@ -52,6 +52,11 @@ plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, 
   t.portion_items = ((1ull << 30) - 1) / t.tile_items * t.tile_items;
   t.num_portions  = ceil_div(n, t.portion_items);
   t.total_tiles   = ceil_div(n, t.tile_items);
+  // Look-back rows are sized for the smaller tile of the two pass kernels, so the size a
+  // caller queried is enough whichever kernel the buffers' alignment selects.
+  const uint64_t min_tile = std::min<uint64_t>(uint64_t(pol.persistent_tpb) * pol.persistent_items,
+                                               uint64_t(pol.onesweep_tpb) * pol.onesweep_items);
+  const uint64_t lookback_rows = ceil_div(n, min_tile) + t.num_portions;
 
   size_t off     = 0;
   t.ctrl_off     = off;
@@ -60,7 +65,7 @@ plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, 
   t.bins_off = off;
   off += align_up(8 * size_t(t.num_passes) * t.num_portions * RADIX_DIGITS, 256);
   t.lookback_off   = off;
-  t.lookback_words = size_t(t.total_tiles) * RADIX_DIGITS;
+  t.lookback_words = size_t(lookback_rows) * RADIX_DIGITS;
   off += align_up(2 * 4 * t.lookback_words, 256);
   t.keys_tmp_off = off;
   if (need_tmp)

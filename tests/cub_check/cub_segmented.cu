@@ -2,7 +2,7 @@
 // binary inputs, to pin the segmented-sort oracle against CUB itself on the GPU machine.
 // Test infrastructure only (compiled there by tests/test_cub_segmented_gpu.py).
 //
-// usage: cub_segmented <n> <num_segments> <descending> <in.bin> <out.bin>
+// usage: cub_segmented <n> <num_segments> <descending> <in.bin> <out.bin> [timing reps]
 //   in.bin  = n f32 keys, n i32 values, num_segments i32 begin offsets, num_segments i32 end offsets
 //   out.bin = n f32 keys, n i32 values (positions outside segments keep the input)
 #include <cub/device/device_segmented_sort.cuh>
@@ -25,10 +25,11 @@
 
 int main(int argc, char** argv)
 {
-  if (argc != 6)
+  if (argc != 6 && argc != 7)
   {
     return 2;
   }
+  const int reps = argc == 7 ? std::atoi(argv[6]) : 0;
   const long n    = std::atol(argv[1]);
   const long nseg = std::atol(argv[2]);
   const bool desc = std::atoi(argv[3]) != 0;
@@ -71,6 +72,23 @@ int main(int argc, char** argv)
     }
   }
   CK(cudaDeviceSynchronize());
+  if (reps > 0)
+  {
+    cudaEvent_t a, z;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&z));
+    CK(cudaEventRecord(a));
+    for (int r = 0; r < reps; ++r)
+    {
+      CK(desc ? cub::DeviceSegmentedSort::StableSortPairsDescending(temp, bytes, ki, ko, vi, vo, n, nseg, db, de)
+              : cub::DeviceSegmentedSort::StableSortPairs(temp, bytes, ki, ko, vi, vo, n, nseg, db, de));
+    }
+    CK(cudaEventRecord(z));
+    CK(cudaEventSynchronize(z));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, a, z));
+    std::printf("{\"impl\": \"cub\", \"ms\": %.4f}\n", ms / reps);
+  }
   CK(cudaMemcpy(keys.data(), ko, n * 4, cudaMemcpyDeviceToHost));
   CK(cudaMemcpy(vals.data(), vo, n * 4, cudaMemcpyDeviceToHost));
   std::ofstream out(argv[5], std::ios::binary);

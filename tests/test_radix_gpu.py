@@ -203,3 +203,30 @@ def test_large_full_size_properties():
     cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
     cnt.index_add_(0, vo.long(), torch.ones_like(vo))
     assert bool((cnt == 1).all())
+
+
+@pytest.mark.parametrize("offset", [1, 3])
+def test_unaligned_buffers_use_the_fallback_pass(oracle, offset):
+    """Buffers that are not 16-byte aligned take the CTA-per-tile pass kernel; the temp size
+    queried for an aligned buffer of the same length must still be enough."""
+    import torch
+
+    from cccl_gb300 import SortOrder, make_radix_sort
+    from gpu_util import from_dev, to_dev
+
+    rng = np.random.default_rng(offset)
+    n = 700_001
+    k = I.uniform_bits(np.uint32, n + offset, rng)
+    v = I.index_values(n + offset)
+    kd, vd = to_dev(k), to_dev(v)
+    ki, vi = kd[offset:], vd[offset:]
+    ko, vo = torch.empty_like(ki), torch.empty_like(vi)
+    s = make_radix_sort(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo, order=SortOrder.ASCENDING)
+    aligned = torch.empty(n, dtype=ki.dtype, device="cuda")
+    nbytes = s(temp_storage=None, d_in_keys=aligned, d_out_keys=aligned, d_in_values=vi, d_out_values=vo, num_items=n)
+    temp = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s(temp_storage=temp, d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo, num_items=n)
+    torch.cuda.synchronize()
+    rk, rv = oracle.radix_sort(k[offset:], v[offset:])
+    assert from_dev(ko, np.uint32).tobytes() == rk.tobytes()
+    assert from_dev(vo, np.uint32).tobytes() == rv.tobytes()
