@@ -142,7 +142,32 @@ class SegmentedSortBuildResult(C.Structure):
     ]
 
 
-# Every symbol the headers under include/cccl/c declare.
+class LearnedSortBuildResult(C.Structure):
+    _fields_ = [
+        ("cc", C.c_int),
+        ("key_type", TypeInfo),
+        ("value_type", TypeInfo),
+        ("order", C.c_int),
+        ("radix_library", C.c_void_p),
+        ("segmented_library", C.c_void_p),
+        ("learned_library", C.c_void_p),
+        ("setup", C.c_void_p),
+        ("setup_size", C.c_size_t),
+    ]
+
+
+class LearnedSortStats(C.Structure):
+    _fields_ = [
+        ("learned", C.c_int),
+        ("bucket_log2", C.c_int),
+        ("partition_passes", C.c_int),
+        ("block_buckets", C.c_uint32),
+        ("device_buckets", C.c_uint32),
+        ("device_items", C.c_uint64),
+    ]
+
+
+# Every symbol the headers under include/ declare.
 EXPORTED_SYMBOLS = [
     "cccl_serialization_buffer_free",
     "cccl_device_radix_sort_build",
@@ -165,6 +190,10 @@ EXPORTED_SYMBOLS = [
     "cccl_device_segmented_sort_cleanup",
     "cccl_gb300_set_launch_observer",
     "cccl_gb300_radix_sort_u32_noalloc",
+    "cccl_gb300_learned_sort_build",
+    "cccl_gb300_learned_sort",
+    "cccl_gb300_learned_sort_stats",
+    "cccl_gb300_learned_sort_cleanup",
 ]
 
 NOALLOC_MAX_ITEMS = 1 << 20  # CCCL_GB300_NOALLOC_MAX_ITEMS
@@ -234,6 +263,23 @@ def _declare(lib):
     lib.cccl_gb300_set_launch_observer.restype = None
     lib.cccl_gb300_radix_sort_u32_noalloc.argtypes = [
         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_bool, C.c_void_p]
+    L = P(LearnedSortBuildResult)
+    lib.cccl_gb300_learned_sort_build.argtypes = [L, C.c_int, Iterator, Iterator, C.c_int, C.c_int]
+    lib.cccl_gb300_learned_sort.argtypes = [LearnedSortBuildResult] + list(lib.cccl_device_radix_sort.argtypes[1:])
+    lib.cccl_gb300_learned_sort_stats.argtypes = [
+        LearnedSortBuildResult,
+        C.c_void_p,
+        Iterator,
+        Iterator,
+        Iterator,
+        Iterator,
+        C.c_uint64,
+        C.c_int,
+        C.c_int,
+        C.c_bool,
+        P(LearnedSortStats),
+    ]
+    lib.cccl_gb300_learned_sort_cleanup.argtypes = [L]
     for name in EXPORTED_SYMBOLS:
         if name not in ("cccl_serialization_buffer_free", "cccl_gb300_set_launch_observer"):
             getattr(lib, name).restype = C.c_int

@@ -38,8 +38,18 @@ IMAGES = {
     "seg_k2": "seg_k2.cu",
     "seg_k4": "seg_k4.cu",
     "seg_k8": "seg_k8.cu",
+    "learned_k4": "learned_k4.cu",
+    "learned_k8": "learned_k8.cu",
 }
-HOST_SOURCES = ["images.cpp", "radix_plan.cpp", "radix_sort_abi.cpp", "segmented_plan.cpp", "segmented_sort_abi.cpp"]
+HOST_SOURCES = [
+    "images.cpp",
+    "radix_plan.cpp",
+    "radix_sort_abi.cpp",
+    "segmented_plan.cpp",
+    "segmented_sort_abi.cpp",
+    "learned_plan.cpp",
+    "learned_sort_abi.cpp",
+]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]
 

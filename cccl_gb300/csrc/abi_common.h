@@ -82,6 +82,7 @@ struct image_ref
 };
 image_ref radix_image(int key_bytes); // one cubin per key width
 image_ref segmented_image(int key_bytes); // one cubin per key width
+image_ref learned_image(int key_bytes);   // 4- and 8-byte keys
 
 // ---- key kinds ----
 enum key_kind : int

@@ -15,6 +15,8 @@ extern const unsigned char gb300_img_seg_k1[], gb300_img_seg_k1_end[];
 extern const unsigned char gb300_img_seg_k2[], gb300_img_seg_k2_end[];
 extern const unsigned char gb300_img_seg_k4[], gb300_img_seg_k4_end[];
 extern const unsigned char gb300_img_seg_k8[], gb300_img_seg_k8_end[];
+extern const unsigned char gb300_img_learned_k4[], gb300_img_learned_k4_end[];
+extern const unsigned char gb300_img_learned_k8[], gb300_img_learned_k8_end[];
 }
 
 namespace gb300
@@ -51,6 +53,19 @@ image_ref segmented_image(int key_bytes)
       return {gb300_img_seg_k8, size_t(gb300_img_seg_k8_end - gb300_img_seg_k8)};
     default:
       throw cuda_error(CUDA_ERROR_NOT_SUPPORTED, "no segmented kernels for this key width");
+  }
+}
+
+image_ref learned_image(int key_bytes)
+{
+  switch (key_bytes)
+  {
+    case 4:
+      return {gb300_img_learned_k4, size_t(gb300_img_learned_k4_end - gb300_img_learned_k4)};
+    case 8:
+      return {gb300_img_learned_k8, size_t(gb300_img_learned_k8_end - gb300_img_learned_k8)};
+    default:
+      throw cuda_error(CUDA_ERROR_NOT_SUPPORTED, "the learned sort takes 4- and 8-byte keys");
   }
 }
 

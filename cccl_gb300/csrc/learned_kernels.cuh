@@ -1,0 +1,311 @@
+// Learned-partition sort kernels for sm_103a (no reference counterpart: a new form of the
+// sort beside CUB's plain radix sort, with the same output bit for bit).
+//
+//   sample  : LEARNED_SAMPLE keys at jittered, evenly spaced positions, encoded;
+//   (the sample is sorted by the plain radix sort, which gives every sample key its rank)
+//   fit     : one CTA per leaf fits rank ~ key by least squares over the leaf's sample points;
+//   hist    : one read of the keys: bucket of every key, digit counts of every partition pass;
+//   pass    : the persistent onesweep pass with the bucket id's digits in place of key bits
+//             (stable, so after the passes the keys are grouped by bucket in input order);
+//   bounds  : first index of every bucket, by binary search on the partitioned keys.
+// The buckets are then sorted as segments by the batched segmented sort; a bucket too large
+// for a block sort goes to its plain radix passes.
+//
+// Exactness does not depend on the model: the bucket id is non-decreasing in the encoded
+// key (the -0.0 rule applied first, so -0.0 and +0.0 share a bucket), the partition is
+// stable and every bucket is sorted stably by the full key, so the result is the stable
+// sort of the input by the encoded key, i.e. CUB's.
+#pragma once
+
+#include "radix_kernels.cuh"
+
+namespace gb300
+{
+
+template <class U>
+struct LearnedTables
+{
+  U knot[LEARNED_LEAVES];
+  float slope[LEARNED_LEAVES];
+  float icpt[LEARNED_LEAVES];
+};
+
+template <class U>
+__device__ __forceinline__ void learned_load_tables(const LearnedModel* m, LearnedTables<U>* t)
+{
+  for (int i = threadIdx.x; i < LEARNED_LEAVES; i += blockDim.x)
+  {
+    t->knot[i]  = U(m->knot[i]);
+    t->slope[i] = m->slope[i];
+    t->icpt[i]  = m->icpt[i];
+  }
+}
+
+__device__ __forceinline__ float learned_to_float(uint32_t x)
+{
+  return __uint2float_rn(x);
+}
+
+__device__ __forceinline__ float learned_to_float(unsigned long long x)
+{
+  return __ull2float_rn(x);
+}
+
+// Bucket of an encoded key. Every step is non-decreasing in the key: the leaf search, the
+// conversion of (key - knot) to float, the fused multiply-add with a slope >= 0, the clamp
+// to the leaf's rank range (leaf j's top equals leaf j+1's bottom) and the truncation after
+// scaling by a power of two.
+template <class U, bool FP>
+__device__ __forceinline__ uint32_t
+learned_bucket(U enc, const LearnedTables<U>& t, float scale, uint32_t bmax)
+{
+  const U k = digit_source<U, FP>(enc);
+  int j     = 0;
+#pragma unroll
+  for (int s = LEARNED_LEAVES / 2; s >= 1; s >>= 1)
+  {
+    if (t.knot[j + s] <= k)
+    {
+      j += s;
+    }
+  }
+  const U kn             = t.knot[j];
+  const float x          = k > kn ? learned_to_float(k - kn) : 0.0f;
+  constexpr float span   = float(LEARNED_SAMPLE / LEARNED_LEAVES);
+  const float lo         = float(j) * span;
+  float r                = fmaf(t.slope[j], x, t.icpt[j]);
+  r                      = fminf(fmaxf(r, lo), lo + span);
+  const uint32_t b       = uint32_t(r * scale);
+  return b < bmax ? b : bmax;
+}
+
+__device__ __forceinline__ float learned_scale(int bucket_log2)
+{
+  return exp2f(float(bucket_log2 - LEARNED_SAMPLE_LOG2)); // a power of two: exact
+}
+
+// ---------------------------------------------------------------------------------------
+// sample: thread i takes one key from [i*n/S, (i+1)*n/S) at a hashed offset
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t learned_mix(uint32_t x)
+{
+  // integer finaliser (xorshift-multiply), only to decorrelate the offsets from the input
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+template <int KB, bool FP>
+__device__ __forceinline__ void learned_sample_body(const LearnedSampleParams& p)
+{
+  using U            = typename uint_of<KB>::type;
+  const uint32_t i   = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= uint32_t(LEARNED_SAMPLE))
+  {
+    return;
+  }
+  const unsigned long long n  = p.num_items;
+  const unsigned long long lo = ((unsigned long long) i * n) >> LEARNED_SAMPLE_LOG2;
+  const unsigned long long hi = ((unsigned long long) (i + 1) * n) >> LEARNED_SAMPLE_LOG2;
+  const unsigned long long w  = hi > lo ? hi - lo : 1;
+  unsigned long long pos      = lo + learned_mix(i) % w;
+  pos                         = pos < n ? pos : n - 1;
+  const U raw                 = static_cast<const U*>(p.keys)[pos];
+  static_cast<U*>(p.sample)[i] = digit_source<U, FP>(encode_key<U>(raw, p.codec));
+}
+
+// ---------------------------------------------------------------------------------------
+// fit: CTA j, thread t holds sample point j*P + t (P = LEARNED_FIT_TPB); centred least
+// squares in double precision
+// ---------------------------------------------------------------------------------------
+template <int TPB>
+__device__ __forceinline__ double learned_block_sum(double v, double* scratch)
+{
+  const int lane = threadIdx.x & 31;
+  const int w    = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+  {
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  __syncthreads(); // scratch reuse across calls
+  if (lane == 0)
+  {
+    scratch[w] = v;
+  }
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < TPB / 32; ++k)
+  {
+    s += scratch[k];
+  }
+  return s;
+}
+
+template <int KB>
+__device__ __forceinline__ void learned_fit_body(const LearnedFitParams& p)
+{
+  using U             = typename uint_of<KB>::type;
+  constexpr int P     = LEARNED_FIT_TPB;
+  __shared__ double scratch[P / 32];
+  const int j         = blockIdx.x;
+  const U* s          = static_cast<const U*>(p.sorted_sample);
+  const uint32_t idx  = uint32_t(j) * P + threadIdx.x;
+  const U knot        = s[uint32_t(j) * P];
+  const double x      = double(s[idx] - knot); // sorted: s[idx] >= knot
+  const double y      = double(idx);
+  const double mx     = learned_block_sum<P>(x, scratch) / P;
+  const double my     = learned_block_sum<P>(y, scratch) / P;
+  const double sxx    = learned_block_sum<P>((x - mx) * (x - mx), scratch);
+  const double sxy    = learned_block_sum<P>((x - mx) * (y - my), scratch);
+  if (threadIdx.x == 0)
+  {
+    double slope = sxx > 0.0 ? sxy / sxx : 0.0;
+    if (!(slope >= 0.0) || !isfinite(slope))
+    {
+      slope = 0.0;
+    }
+    double icpt = my - slope * mx;
+    if (!isfinite(icpt))
+    {
+      icpt = my;
+    }
+    p.model->knot[j]  = (unsigned long long) knot;
+    p.model->slope[j] = float(slope);
+    p.model->icpt[j]  = float(icpt);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// hist: digit counts of every partition pass in one read of the keys
+// ---------------------------------------------------------------------------------------
+template <int KB, bool FP, int TPB>
+__device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
+{
+  using U         = typename uint_of<KB>::type;
+  constexpr int R = RADIX_DIGITS;
+  __shared__ uint32_t sh[MAX_PASSES * R];
+  __shared__ LearnedTables<U> tables;
+
+  for (int i = threadIdx.x; i < MAX_PASSES * R; i += TPB)
+  {
+    sh[i] = 0;
+  }
+  learned_load_tables<U>(p.model, &tables);
+  __syncthreads();
+
+  const float scale    = learned_scale(p.bucket_log2);
+  const uint32_t bmax  = (1u << p.bucket_log2) - 1u;
+  const int passes     = p.h.num_passes;
+  auto count_key       = [&](U raw) {
+    const uint32_t b = learned_bucket<U, FP>(encode_key<U>(raw, p.h.codec), tables, scale, bmax);
+#pragma unroll
+    for (int q = 0; q < MAX_PASSES; ++q)
+    {
+      if (q < passes)
+      {
+        atomicAdd(&sh[q * R + ((b >> (8 * q)) & 255u)], 1u);
+      }
+    }
+  };
+  histogram_for_each_key<KB, TPB>(p.h.keys, p.h.num_items, count_key);
+  histogram_finish<TPB>(p.h, sh);
+}
+
+// ---------------------------------------------------------------------------------------
+// pass: hook of the persistent onesweep pass that supplies the bucket id's digit
+// ---------------------------------------------------------------------------------------
+template <class U, bool FP>
+struct LearnedPassHook
+{
+  const LearnedModel* model;
+  float scale;
+  uint32_t bmax;
+  int shift;
+
+  template <int ITEMS>
+  using digits_t = ComputedDigits<ITEMS>;
+
+  static constexpr size_t tables_bytes = round16(sizeof(LearnedTables<U>));
+
+  __device__ __forceinline__ void setup(unsigned char* extra) const
+  {
+    learned_load_tables<U>(model, reinterpret_cast<LearnedTables<U>*>(extra));
+  }
+
+  template <class K, int ITEMS>
+  __device__ __forceinline__ void
+  compute(const K (&keys)[ITEMS], uint32_t valid, int wofs, ComputedDigits<ITEMS>& dg, unsigned char* extra) const
+  {
+    const auto& t = *reinterpret_cast<const LearnedTables<U>*>(extra);
+    dg.stage      = extra + tables_bytes;
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      const uint32_t idx = uint32_t(wofs + i * 32);
+      dg.d[i] = idx < valid ? (learned_bucket<U, FP>(keys[i], t, scale, bmax) >> shift) & 255u : 255u;
+    }
+  }
+};
+
+template <int KB, int VB, bool FP>
+__device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
+{
+  using U             = typename uint_of<KB>::type;
+  constexpr int TPB   = persistent_tpb(KB, VB);
+  constexpr int ITEMS = learned_items(KB, VB);
+  constexpr size_t EXTRA = learned_extra_bytes(KB, VB, ITEMS);
+  static_assert(LearnedPassHook<U, FP>::tables_bytes == round16(size_t(LEARNED_LEAVES) * (KB + 8)),
+                "learned tables layout");
+  const LearnedPassHook<U, FP> hook{p.model, learned_scale(p.bucket_log2), (1u << p.bucket_log2) - 1u, p.digit_shift};
+  onesweep_persistent_body<KB, VB, FP, TPB, ITEMS, true, LearnedPassHook<U, FP>, EXTRA>(p.os, hook);
+}
+
+// ---------------------------------------------------------------------------------------
+// bounds: thread b finds the first index whose key is in a bucket >= b
+// ---------------------------------------------------------------------------------------
+template <int KB, bool FP>
+__device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p)
+{
+  using U = typename uint_of<KB>::type;
+  __shared__ LearnedTables<U> tables;
+  learned_load_tables<U>(p.model, &tables);
+  __syncthreads();
+
+  const unsigned long long nb = 1ull << p.bucket_log2;
+  const unsigned long long b  = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x;
+  if (b > nb)
+  {
+    return;
+  }
+  const unsigned long long n = p.num_items;
+  if (b == 0 || b == nb)
+  {
+    p.bounds[b] = b == 0 ? 0ull : n;
+    return;
+  }
+  const float scale   = learned_scale(p.bucket_log2);
+  const uint32_t bmax = uint32_t(nb - 1);
+  const U* keys       = static_cast<const U*>(p.keys);
+  unsigned long long lo = 0, hi = n;
+  while (lo < hi)
+  {
+    const unsigned long long mid = (lo + hi) >> 1;
+    const uint32_t bk = learned_bucket<U, FP>(encode_key<U>(keys[mid], p.codec), tables, scale, bmax);
+    if (bk < uint32_t(b))
+    {
+      lo = mid + 1;
+    }
+    else
+    {
+      hi = mid;
+    }
+  }
+  p.bounds[b] = lo;
+}
+
+} // namespace gb300

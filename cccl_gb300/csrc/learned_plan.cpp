@@ -1,0 +1,395 @@
+// Host dispatcher of the learned-partition sort (see learned_plan.h).
+//
+// No reference counterpart: it is a second form of DeviceRadixSort::SortKeys/SortPairs with
+// the same result and the same DoubleBuffer selector as the plain sort
+// (cub/cub/device/dispatch/dispatch_radix_sort.cuh:1698-1948 leaves the result of a
+// full-width sort of k-byte keys after k 8-bit passes, i.e. in the current buffer when k is
+// even). Bucket count: about 2^LEARNED_BUCKET_ITEMS_LOG2 keys per bucket, so that nearly
+// every bucket fits a block sort; the partition needs ceil(log2(buckets) / 8) stable passes.
+#include "learned_plan.h"
+
+#include <algorithm>
+
+#include "abi_common.h"
+#include "sort_policy.h"
+
+namespace gb300
+{
+
+namespace
+{
+uint64_t ceil_div(uint64_t a, uint64_t b)
+{
+  return (a + b - 1) / b;
+}
+
+int ceil_log2(uint64_t x)
+{
+  int l = 0;
+  while ((1ull << l) < x)
+  {
+    ++l;
+  }
+  return l;
+}
+
+bool aligned16(const void* p)
+{
+  return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+
+// Stand-in buffers for size queries: 256-byte aligned, never dereferenced.
+void* fake_ptr(int i)
+{
+  return reinterpret_cast<void*>(uintptr_t(256) * uintptr_t(i + 1));
+}
+
+SegmentedCall bucket_sort_call(const LearnedSetup& s, const RadixCall& c, const LearnedTempPlan& t)
+{
+  SegmentedCall sc{};
+  sc.keys[0]       = fake_ptr(0);
+  sc.keys[1]       = fake_ptr(1);
+  sc.values[0]     = (s.value_bytes > 0 && c.values[0] != nullptr) ? fake_ptr(2) : nullptr;
+  sc.values[1]     = sc.values[0] != nullptr ? fake_ptr(3) : nullptr;
+  sc.num_items     = c.num_items;
+  sc.num_segments  = 1ull << t.bucket_log2;
+  sc.begin_offsets = fake_ptr(4);
+  sc.end_offsets   = fake_ptr(5);
+  sc.offsets_64    = 1;
+  sc.overwrite     = true;
+  sc.descending    = c.descending;
+  sc.stream        = c.stream;
+  sc.target        = 0;
+  return sc;
+}
+} // namespace
+
+LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
+{
+  LearnedTempPlan t{};
+  const int kb        = s.key_bytes;
+  const int vb        = s.value_bytes;
+  const bool has_vals = vb > 0 && c.values[0] != nullptr;
+  const bool aligned  = aligned16(c.keys[0]) && aligned16(c.keys[1])
+                    && (!has_vals || (aligned16(c.values[0]) && aligned16(c.values[1])));
+  t.learned = c.num_items >= LEARNED_MIN_ITEMS && c.begin_bit == 0 && c.end_bit == 8 * kb && aligned
+           && (kb == 4 || kb == 8) && (vb == 0 || vb == 4 || vb == 8);
+  if (!t.learned)
+  {
+    return t;
+  }
+  const uint64_t n = c.num_items;
+  t.bucket_log2    = std::clamp(ceil_log2(n) - LEARNED_BUCKET_ITEMS_LOG2, 8, LEARNED_MAX_BUCKET_LOG2);
+  t.passes         = (t.bucket_log2 + RADIX_BITS - 1) / RADIX_BITS;
+  t.tile_items     = uint64_t(s.pass_tpb) * s.pass_items;
+  t.portion_items  = ((1ull << 30) - 1) / t.tile_items * t.tile_items; // 30-bit look-back counts
+  t.num_portions   = ceil_div(n, t.portion_items);
+  const uint64_t lookback_rows = ceil_div(n, t.tile_items) + t.num_portions;
+
+  size_t off   = 0;
+  t.ctrl_off   = off;
+  t.ctrl_bytes = align_up(sizeof(SortControl) + 4 * size_t(t.passes) * t.num_portions, 256);
+  off += t.ctrl_bytes;
+  t.bins_off = off;
+  off += align_up(8 * size_t(t.passes) * t.num_portions * RADIX_DIGITS, 256);
+  t.lookback_off   = off;
+  t.lookback_words = size_t(lookback_rows) * RADIX_DIGITS;
+  off += align_up(2 * 4 * t.lookback_words, 256);
+  t.model_off = off;
+  off += align_up(sizeof(LearnedModel), 256);
+  t.sample_off = off;
+  off += 2 * align_up(size_t(LEARNED_SAMPLE) * kb, 256);
+  t.sample_temp_off   = off;
+  t.sample_temp_bytes = plan_radix_temp(s.sample_pol, LEARNED_SAMPLE, 0, 8 * kb, false, true).total_bytes;
+  off += align_up(t.sample_temp_bytes, 256);
+  t.bounds_off = off;
+  off += align_up(8 * ((size_t(1) << t.bucket_log2) + 1), 256);
+  t.keys_tmp_off = off;
+  if (!c.overwrite)
+  {
+    off += align_up(size_t(n) * kb, 256);
+  }
+  t.values_tmp_off = off;
+  if (!c.overwrite && has_vals)
+  {
+    off += align_up(size_t(n) * vb, 256);
+  }
+  t.seg_off = off;
+  // the buffer the bucket sort must land in changes its pass count: size for both
+  t.seg_bytes = 0;
+  for (int target = 0; target < 2; ++target)
+  {
+    SegmentedCall sc      = bucket_sort_call(s, c, t);
+    size_t bytes          = 0;
+    sc.d_temp_storage     = nullptr;
+    sc.temp_storage_bytes = &bytes;
+    sc.target             = target;
+    int sel               = 0;
+    segmented_sort_dispatch(s.seg_pol, s.seg_ks, sc, &sel);
+    t.seg_bytes = std::max(t.seg_bytes, bytes);
+  }
+  off += align_up(t.seg_bytes, 256);
+  t.fallback_off   = off;
+  t.fallback_bytes = 0;
+  if (n >= (1ull << 30))
+  {
+    t.fallback_bytes = plan_radix_temp(s.plain_pol, n, 0, 8 * kb, true, true).total_bytes;
+    off += align_up(t.fallback_bytes, 256);
+  }
+  t.total_bytes = off;
+  return t;
+}
+
+void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selector)
+{
+  *selector             = 0;
+  const LearnedTempPlan t = plan_learned_temp(s, c);
+  if (!t.learned)
+  {
+    radix_sort_dispatch(s.plain_pol, s.plain_ks, c, selector);
+    return;
+  }
+  if (c.d_temp_storage == nullptr)
+  {
+    *c.temp_storage_bytes = t.total_bytes;
+    return;
+  }
+  const int kb        = s.key_bytes;
+  const int vb        = s.value_bytes;
+  const bool has_vals = vb > 0 && c.values[0] != nullptr;
+  const uint64_t n    = c.num_items;
+  if (*c.temp_storage_bytes < t.total_bytes)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "temp storage is smaller than the size query returned");
+  }
+  if ((reinterpret_cast<uintptr_t>(c.d_temp_storage) & 255) != 0)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "temp storage is not 256-byte aligned");
+  }
+  if (c.keys[0] == nullptr || c.keys[1] == nullptr || (has_vals && c.values[1] == nullptr))
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "key/value buffer is null");
+  }
+
+  auto* base          = static_cast<unsigned char*>(c.d_temp_storage);
+  auto* ctrl          = reinterpret_cast<SortControl*>(base + t.ctrl_off);
+  auto* tile_ctrs     = reinterpret_cast<uint32_t*>(base + t.ctrl_off + sizeof(SortControl));
+  auto* bins          = reinterpret_cast<unsigned long long*>(base + t.bins_off);
+  uint32_t* lb[2]     = {reinterpret_cast<uint32_t*>(base + t.lookback_off),
+                         reinterpret_cast<uint32_t*>(base + t.lookback_off) + t.lookback_words};
+  auto* model         = reinterpret_cast<LearnedModel*>(base + t.model_off);
+  void* sample[2]     = {base + t.sample_off, base + t.sample_off + align_up(size_t(LEARNED_SAMPLE) * kb, 256)};
+  auto* bounds        = reinterpret_cast<unsigned long long*>(base + t.bounds_off);
+  void* keys_tmp      = base + t.keys_tmp_off;
+  void* values_tmp    = base + t.values_tmp_off;
+  const KeyCodec codec = make_codec(s.key_kind, kb, c.descending);
+  const int sms        = sm_count();
+  const int plain_passes = int(ceil_div(uint64_t(8 * kb), RADIX_BITS));
+  const int final_sel    = plain_passes & 1; // the plain sort's selector
+
+  // 1. zero the control block
+  {
+    InitParams p{};
+    p.words     = reinterpret_cast<uint32_t*>(ctrl);
+    p.num_words = t.ctrl_bytes / 4;
+    launch("learned_init", s.lk.init, unsigned(std::min<uint64_t>(ceil_div(p.num_words, 256), 1024)), 256, 0,
+           c.stream, p);
+  }
+  // 2. sample, 3. its plain radix sort (exact ranks), 4. least-squares fit per leaf
+  {
+    LearnedSampleParams p{};
+    p.keys      = c.keys[0];
+    p.num_items = n;
+    p.sample    = sample[0];
+    p.codec     = codec;
+    launch("learned_sample", s.lk.sample, unsigned(LEARNED_SAMPLE / 256), 256, 0, c.stream, p);
+  }
+  int ssel = 0;
+  {
+    RadixCall sc{};
+    sc.keys[0]            = sample[0];
+    sc.keys[1]            = sample[1];
+    sc.num_items          = LEARNED_SAMPLE;
+    sc.begin_bit          = 0;
+    sc.end_bit            = 8 * kb;
+    sc.overwrite          = true;
+    sc.descending         = false;
+    sc.d_temp_storage     = base + t.sample_temp_off;
+    size_t bytes          = t.sample_temp_bytes;
+    sc.temp_storage_bytes = &bytes;
+    sc.stream             = c.stream;
+    radix_sort_dispatch(s.sample_pol, s.sample_ks, sc, &ssel);
+  }
+  {
+    LearnedFitParams p{};
+    p.sorted_sample = sample[ssel];
+    p.model         = model;
+    launch("learned_fit", s.lk.fit, unsigned(LEARNED_LEAVES), unsigned(LEARNED_FIT_TPB), 0, c.stream, p);
+  }
+  // 5. digit counts of every partition pass (and pass 0's look-back cleared)
+  {
+    LearnedHistParams p{};
+    p.h.keys           = c.keys[0];
+    p.h.num_items      = n;
+    p.h.codec          = codec;
+    p.h.begin_bit      = 0;
+    p.h.end_bit        = t.bucket_log2;
+    p.h.num_passes     = t.passes;
+    p.h.num_portions   = int(t.num_portions);
+    p.h.ctrl           = ctrl;
+    p.h.bins           = bins;
+    p.h.lookback_clear = lb[0];
+    p.h.lookback_words = t.lookback_words;
+    p.model            = model;
+    p.bucket_log2      = t.bucket_log2;
+    const uint64_t want = ceil_div(n, uint64_t(HISTOGRAM_TPB) * (16 / kb) * 4);
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sms) * 4)));
+    launch("learned_hist", s.lk.hist, grid, unsigned(HISTOGRAM_TPB), 0, c.stream, p);
+  }
+  // 6. stable partition passes on the bucket id, low digit first
+  const int P = t.passes;
+  void* ksrc[MAX_PASSES];
+  void* kdst[MAX_PASSES];
+  void* vsrc[MAX_PASSES];
+  void* vdst[MAX_PASSES];
+  for (int q = 0; q < P; ++q)
+  {
+    if (c.overwrite)
+    {
+      ksrc[q] = c.keys[q & 1];
+      kdst[q] = c.keys[(q + 1) & 1];
+      vsrc[q] = c.values[q & 1];
+      vdst[q] = c.values[(q + 1) & 1];
+    }
+    else
+    {
+      const bool to_tmp = ((P - 1 - q) % 2) == 0; // the last pass lands in the temp buffers
+      kdst[q]           = to_tmp ? keys_tmp : c.keys[1];
+      vdst[q]           = to_tmp ? values_tmp : c.values[1];
+      ksrc[q]           = q == 0 ? c.keys[0] : kdst[q - 1];
+      vsrc[q]           = q == 0 ? c.values[0] : vdst[q - 1];
+    }
+  }
+  const uint64_t tiles_per_portion = t.portion_items / t.tile_items;
+  const unsigned pass_grid_cap = unsigned(sms * occupancy(s.lk.pass, s.pass_tpb, s.pass_smem));
+  for (int q = 0; q < P; ++q)
+  {
+    for (uint64_t pi = 0; pi < t.num_portions; ++pi)
+    {
+      const uint64_t first = pi * t.portion_items;
+      const uint64_t items = std::min<uint64_t>(n - first, t.portion_items);
+      LearnedPassParams lp{};
+      OnesweepParams& op  = lp.os;
+      op.keys_in          = static_cast<const unsigned char*>(ksrc[q]) + first * kb;
+      op.keys_out         = kdst[q];
+      op.values_in        = has_vals ? static_cast<const unsigned char*>(vsrc[q]) + first * vb : nullptr;
+      op.values_out       = has_vals ? vdst[q] : nullptr;
+      op.portion_begin    = first;
+      op.num_items_total  = n;
+      op.portion_items    = uint32_t(items);
+      op.portion_tiles    = uint32_t(ceil_div(items, t.tile_items));
+      op.tile_row_base    = uint32_t(pi * tiles_per_portion);
+      op.lookback         = lb[q & 1];
+      op.lookback_next    = (q + 1 < P) ? lb[(q + 1) & 1] : nullptr;
+      op.tile_counter     = tile_ctrs + (size_t(q) * t.num_portions + pi);
+      op.bins             = bins + (size_t(q) * t.num_portions + pi) * RADIX_DIGITS;
+      op.bins_next        = (pi + 1 < t.num_portions) ? bins + (size_t(q) * t.num_portions + pi + 1) * RADIX_DIGITS : nullptr;
+      op.status           = &ctrl->status;
+      op.codec            = codec;
+      op.current_bit      = q * RADIX_BITS;
+      op.num_bits         = std::min(RADIX_BITS, t.bucket_log2 - q * RADIX_BITS);
+      op.encode_in        = q == 0;
+      op.decode_out       = q == P - 1;
+      lp.model            = model;
+      lp.bucket_log2      = t.bucket_log2;
+      lp.digit_shift      = q * RADIX_BITS;
+      const unsigned grid = std::min<unsigned>(op.portion_tiles, pass_grid_cap);
+      launch_cooperative("learned_pass", s.lk.pass, grid, unsigned(s.pass_tpb), s.pass_smem, c.stream, lp);
+    }
+  }
+  void* part_keys = kdst[P - 1];
+  void* part_vals = has_vals ? vdst[P - 1] : nullptr;
+  // 7. first index of every bucket
+  {
+    LearnedBoundsParams p{};
+    p.keys        = part_keys;
+    p.num_items   = n;
+    p.model       = model;
+    p.bounds      = bounds;
+    p.codec       = codec;
+    p.bucket_log2 = t.bucket_log2;
+    const uint64_t threads = (1ull << t.bucket_log2) + 1;
+    launch("learned_bounds", s.lk.bounds, unsigned(ceil_div(threads, LEARNED_BOUNDS_TPB)), LEARNED_BOUNDS_TPB, 0,
+           c.stream, p);
+  }
+  // 8. every bucket sorted as a segment; the result lands where the plain sort puts it
+  {
+    void* final_keys  = c.overwrite ? c.keys[final_sel] : c.keys[1];
+    void* other_keys  = part_keys == c.keys[0] ? c.keys[1] : part_keys == c.keys[1] ? c.keys[0] : c.keys[1];
+    void* other_vals  = nullptr;
+    if (has_vals)
+    {
+      other_vals = part_vals == c.values[0] ? c.values[1] : part_vals == c.values[1] ? c.values[0] : c.values[1];
+    }
+    SegmentedCall sc      = bucket_sort_call(s, c, t);
+    sc.keys[0]            = part_keys;
+    sc.keys[1]            = other_keys;
+    sc.values[0]          = part_vals;
+    sc.values[1]          = other_vals;
+    sc.begin_offsets      = bounds;
+    sc.end_offsets        = bounds + 1;
+    sc.target             = final_keys == part_keys ? 0 : 1;
+    sc.d_temp_storage     = base + t.seg_off;
+    size_t bytes          = t.seg_bytes;
+    sc.temp_storage_bytes = &bytes;
+    int seg_sel           = 0;
+    segmented_sort_dispatch(s.seg_pol, s.seg_ks, sc, &seg_sel);
+    // 9. a bucket of 2^30 or more keys was left unsorted: a stable sort of the partitioned
+    // keys equals the stable sort of the input (the partition keeps equal keys in order),
+    // so the plain radix sort of them into the final buffer finishes the job
+    if (t.fallback_bytes > 0)
+    {
+      RadixCall fc{};
+      fc.keys[0]            = part_keys;
+      fc.keys[1]            = final_keys;
+      fc.values[0]          = part_vals;
+      fc.values[1]          = has_vals ? (c.overwrite ? c.values[final_sel] : c.values[1]) : nullptr;
+      fc.num_items          = n;
+      fc.begin_bit          = 0;
+      fc.end_bit            = 8 * kb;
+      fc.overwrite          = false;
+      fc.descending         = c.descending;
+      fc.d_temp_storage     = base + t.fallback_off;
+      size_t fbytes         = t.fallback_bytes;
+      fc.temp_storage_bytes = &fbytes;
+      fc.stream             = c.stream;
+      fc.gate.gate          = reinterpret_cast<const uint32_t*>(base + t.seg_off) + SEG_CTR_STATUS;
+      fc.gate.gate_mask     = STATUS_BAD_SEGMENT;
+      int fsel              = 0;
+      radix_sort_dispatch(s.plain_pol, s.plain_ks, fc, &fsel);
+    }
+  }
+  *selector = final_sel;
+}
+
+LearnedStats learned_sort_stats(const LearnedSetup& s, const RadixCall& c)
+{
+  LearnedStats st{};
+  const LearnedTempPlan t = plan_learned_temp(s, c);
+  st.learned              = t.learned ? 1 : 0;
+  if (!t.learned || c.d_temp_storage == nullptr)
+  {
+    return st;
+  }
+  st.bucket_log2      = t.bucket_log2;
+  st.partition_passes = t.passes;
+  uint32_t w[SEG_CTR_WORDS];
+  check(cuMemcpyDtoH(w, CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.seg_off), sizeof(w)),
+        "cuMemcpyDtoH(learned stats)");
+  st.block_buckets  = w[SEG_CTR_SMALL] + w[SEG_CTR_MEDIUM] + w[SEG_CTR_BLOCK_S] + w[SEG_CTR_BLOCK_L];
+  st.device_buckets = w[SEG_CTR_DEVICE];
+  std::memcpy(&st.device_items, &w[SEG_CTR_DEVICE_ITEMS], sizeof(st.device_items));
+  return st;
+}
+
+} // namespace gb300

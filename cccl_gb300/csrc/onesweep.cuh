@@ -46,10 +46,29 @@ struct OnesweepSmem
 // misc words: [0] tile id, [1] tile failed (stores disabled), [2] sticky failure of the
 // CTA, [8..15] scan scratch, [16..19] two mbarriers (persistent kernel).
 
+// Where a pass takes its digits from.
+//   RadixDigits: bits [current_bit, current_bit + num_bits) of the encoded key, recomputed
+//     wherever needed (histogram, ranking, write-out);
+//   ComputedDigits: one digit per key supplied by the caller (a digit that is not a bit
+//     field of the key, e.g. a model's bucket id). Padding keys of a partial tile must get
+//     digit 255. The digits are staged next to the keys so the write-out reads them back.
+struct RadixDigits
+{
+  static constexpr bool computed = false;
+};
+
+template <int ITEMS>
+struct ComputedDigits
+{
+  static constexpr bool computed = true;
+  uint32_t d[ITEMS];
+  uint8_t* stage; // [TILE] digit of every staging slot
+};
+
 // Per-tile steps 1-4. Preconditions: whist is zero, keys[] hold the tile's encoded keys
 // (padding keys of a partial tile are all-ones), misc[1] says whether stores are
 // disabled. load_values(vals) is called once after the ranking to fill the values.
-template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE, class LoadValues>
+template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE, class LoadValues, class Digits = RadixDigits>
 __device__ __forceinline__ void onesweep_tile(
   const OnesweepParams& p,
   const uint32_t tile,
@@ -60,7 +79,8 @@ __device__ __forceinline__ void onesweep_tile(
   uint32_t* misc,
   typename uint_of<KB>::type* kstage,
   typename value_word<VB>::type* vstage,
-  LoadValues&& load_values)
+  LoadValues&& load_values,
+  const Digits& dg = Digits{})
 {
   using U            = typename uint_of<KB>::type;
   using V            = typename value_word<VB>::type;
@@ -69,6 +89,7 @@ __device__ __forceinline__ void onesweep_tile(
   constexpr int R    = RADIX_DIGITS;
   static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
   static_assert(STABLE || VB == 0, "pairs need a stable pass");
+  static_assert(STABLE || !Digits::computed, "computed digits are ranked stably");
 
   const int tid        = threadIdx.x;
   const int warp       = tid >> 5;
@@ -76,7 +97,14 @@ __device__ __forceinline__ void onesweep_tile(
   const int bit        = p.current_bit;
   const uint32_t dmask = (1u << p.num_bits) - 1u;
 
-  warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+  if constexpr (Digits::computed)
+  {
+    warp_histogram_digits<ITEMS>(dg.d, whist + warp * R);
+  }
+  else
+  {
+    warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+  }
   __syncthreads();
 
   // ---- tile positions; publish the tile's digit counts; look-back ----
@@ -154,7 +182,11 @@ __device__ __forceinline__ void onesweep_tile(
   // ---- stable ranks, scatter into the staging tile ----
   uint32_t pos[ITEMS];
   __syncwarp(); // reconverge after the divergent look-back before the warp votes
-  if (STABLE || !full) // a partial tile's padding keys must rank after its real keys
+  if constexpr (Digits::computed)
+  {
+    warp_rank_stable_digits<ITEMS>(dg.d, pos, whist + warp * R);
+  }
+  else if (STABLE || !full) // a partial tile's padding keys must rank after its real keys
   {
     warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
   }
@@ -166,6 +198,14 @@ __device__ __forceinline__ void onesweep_tile(
   for (int i = 0; i < ITEMS; ++i)
   {
     kstage[pos[i]] = keys[i];
+  }
+  if constexpr (Digits::computed)
+  {
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      dg.stage[pos[i]] = uint8_t(dg.d[i]);
+    }
   }
   if constexpr (VB > 0)
   {
@@ -191,8 +231,16 @@ __device__ __forceinline__ void onesweep_tile(
     const uint32_t s = j * TPB + threadIdx.x;
     if (full || s < valid)
     {
-      const U k         = kstage[s];
-      const uint32_t d  = extract_digit<U, FP>(k, bit, dmask);
+      const U k = kstage[s];
+      uint32_t d;
+      if constexpr (Digits::computed)
+      {
+        d = dg.stage[s];
+      }
+      else
+      {
+        d = extract_digit<U, FP>(k, bit, dmask);
+      }
       const long long g = gdelta[d] + (long long) s;
       if ((unsigned long long) g < out_limit)
       {
@@ -283,6 +331,10 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
   U* kstage         = reinterpret_cast<U*>(smem + L::kstage_off);
   V* vstage         = reinterpret_cast<V*>(smem + L::vstage_off);
 
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
   const int tid = threadIdx.x;
   if (tid == 0)
   {
@@ -312,7 +364,7 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
 // Persistent kernel: tiles blockIdx.x + k * gridDim.x, the next tile prefetched into
 // shared memory by bulk async copies while the current one is processed.
 // ---------------------------------------------------------------------------------------
-template <int KB, int VB, int TPB, int ITEMS>
+template <int KB, int VB, int TPB, int ITEMS, size_t EXTRA = 0>
 struct PersistentSmem
 {
   using U                   = typename uint_of<KB>::type;
@@ -326,13 +378,26 @@ struct PersistentSmem
   static constexpr size_t kbytes     = ((sizeof(U) * TILE + 15) / 16) * 16;
   static constexpr size_t vbytes     = VB > 0 ? sizeof(V) * TILE : 0;
   static constexpr size_t buf_bytes  = kbytes + vbytes; // keys, then values; input and staging
-  static constexpr size_t bytes      = buf_off + 2 * buf_bytes;
+  static constexpr size_t extra_off  = buf_off + 2 * buf_bytes; // the pass hook's own region
+  static constexpr size_t bytes      = extra_off + EXTRA;
 };
 
-template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE>
-__device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p)
+// Pass hook of the persistent kernel: the plain radix pass has none. A hook may fill its
+// shared-memory region once per CTA (setup) and supply computed digits per tile.
+struct PlainPassHook
 {
-  using L            = PersistentSmem<KB, VB, TPB, ITEMS>;
+  template <int ITEMS>
+  using digits_t = RadixDigits;
+  __device__ __forceinline__ void setup(unsigned char*) const {}
+  template <class U, int ITEMS>
+  __device__ __forceinline__ void compute(const U (&)[ITEMS], uint32_t, int, RadixDigits&, unsigned char*) const
+  {}
+};
+
+template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE, class Hook = PlainPassHook, size_t EXTRA = 0>
+__device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p, const Hook& hook = Hook{})
+{
+  using L            = PersistentSmem<KB, VB, TPB, ITEMS, EXTRA>;
   using U            = typename L::U;
   using V            = typename L::V;
   constexpr int NW   = L::NW;
@@ -351,6 +416,10 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
     return reinterpret_cast<V*>(smem + L::buf_off + size_t(b) * L::buf_bytes + L::kbytes);
   };
 
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
   const int tid         = threadIdx.x;
   const int wofs        = (tid >> 5) * ITEMS * 32 + (tid & 31);
   const uint32_t ntiles = p.portion_tiles;
@@ -376,6 +445,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
       issue(blockIdx.x, 0);
     }
   }
+  hook.setup(smem + L::extra_off);
   __syncthreads();
 
   uint32_t parity = 0; // bit b: phase parity to wait for on buffer b
@@ -438,6 +508,8 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
         load_tile_values_global<VB, TPB, ITEMS>(p, tile_first, valid, vals);
       }
     }
+    typename Hook::template digits_t<ITEMS> dg;
+    hook.template compute<U, ITEMS>(keys, valid, wofs, dg, smem + L::extra_off);
     if (!data_ok)
     {
       // the copy never completed: this CTA stores nothing from here on
@@ -456,7 +528,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
             out[i] = vals[i];
           }
         }
-      });
+      }, dg);
     __syncthreads(); // staging tile written out; whist/gdelta/misc free for the next tile
   }
 }

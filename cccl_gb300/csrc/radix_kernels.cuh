@@ -33,6 +33,10 @@ namespace gb300
 // ---------------------------------------------------------------------------------------
 __device__ __forceinline__ void init_body(const InitParams& p)
 {
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
   for (unsigned long long i = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; i < p.num_words;
        i += (unsigned long long) gridDim.x * blockDim.x)
   {
@@ -40,85 +44,15 @@ __device__ __forceinline__ void init_body(const InitParams& p)
   }
 }
 
-// ---------------------------------------------------------------------------------------
-// histogram: counts of every pass's digit in one read; the last CTA writes the exclusive
-// prefix (global digit bases) of portion 0 for every pass. Also clears pass 0's look-back.
-// ---------------------------------------------------------------------------------------
-template <int KB, bool FP, int TPB>
-__device__ __forceinline__ void histogram_body(const HistogramParams& p)
+// Second half of every all-pass histogram kernel: clears pass 0's look-back buffer, adds
+// this CTA's shared counts (sh[pass * 256 + digit]) to the global ones, and the last CTA
+// to finish writes each pass's exclusive prefix (portion 0's digit bases).
+template <int TPB>
+__device__ __forceinline__ void histogram_finish(const HistogramParams& p, const uint32_t* sh)
 {
-  using U          = typename uint_of<KB>::type;
-  constexpr int R  = RADIX_DIGITS;
-  constexpr int VEC = 16 / KB;
-  __shared__ uint32_t sh[MAX_PASSES * R];
+  constexpr int R = RADIX_DIGITS;
   __shared__ uint32_t last_flag;
-
   const int tid = threadIdx.x;
-  for (int i = tid; i < MAX_PASSES * R; i += TPB)
-  {
-    sh[i] = 0;
-  }
-  __syncthreads();
-
-  int shift[MAX_PASSES];
-  uint32_t mask[MAX_PASSES];
-#pragma unroll
-  for (int q = 0; q < MAX_PASSES; ++q)
-  {
-    const int b  = p.begin_bit + q * RADIX_BITS;
-    const int nb = min(RADIX_BITS, p.end_bit - b);
-    shift[q]     = b;
-    mask[q]      = (q < p.num_passes) ? ((1u << nb) - 1u) : 0u;
-  }
-
-  auto count_key = [&](U raw) {
-    const U t = encode_key<U>(raw, p.codec);
-#pragma unroll
-    for (int q = 0; q < MAX_PASSES; ++q)
-    {
-      if (q < p.num_passes)
-      {
-        atomicAdd(&sh[q * R + extract_digit<U, FP>(t, shift[q], mask[q])], 1u);
-      }
-    }
-  };
-
-  const U* keys             = static_cast<const U*>(p.keys);
-  const unsigned long long n = p.num_items;
-  // scalar head up to 16-byte alignment, vector body, scalar tail
-  const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
-  unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
-  if (head > n)
-  {
-    head = n;
-  }
-  const unsigned long long nvec = (n - head) / VEC;
-  const unsigned long long body_end = head + nvec * VEC;
-  if (blockIdx.x == 0)
-  {
-    for (unsigned long long i = tid; i < head; i += TPB)
-    {
-      count_key(keys[i]);
-    }
-    for (unsigned long long i = body_end + tid; i < n; i += TPB)
-    {
-      count_key(keys[i]);
-    }
-  }
-  const uint4* vkeys = reinterpret_cast<const uint4*>(keys + head);
-  for (unsigned long long v = blockIdx.x * (unsigned long long) TPB + tid; v < nvec;
-       v += (unsigned long long) gridDim.x * TPB)
-  {
-    const uint4 w = __ldcs(vkeys + v);
-    U k[VEC];
-    memcpy(k, &w, 16);
-#pragma unroll
-    for (int j = 0; j < VEC; ++j)
-    {
-      count_key(k[j]);
-    }
-  }
-
   // clear the look-back buffer of pass 0
   for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < p.lookback_words;
        i += (unsigned long long) gridDim.x * TPB)
@@ -178,6 +112,98 @@ __device__ __forceinline__ void histogram_body(const HistogramParams& p)
       run += c[j];
     }
   }
+}
+
+// Calls fn(key) once for every key of keys[0, n), spread over the grid: a scalar head up
+// to 16-byte alignment and a scalar tail (CTA 0), 16-byte streaming loads in between.
+template <int KB, int TPB, class Fn>
+__device__ __forceinline__ void histogram_for_each_key(const void* keys_v, unsigned long long n, Fn&& fn)
+{
+  using U           = typename uint_of<KB>::type;
+  constexpr int VEC = 16 / KB;
+  const int tid     = threadIdx.x;
+  const U* keys     = static_cast<const U*>(keys_v);
+  const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
+  unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
+  if (head > n)
+  {
+    head = n;
+  }
+  const unsigned long long nvec     = (n - head) / VEC;
+  const unsigned long long body_end = head + nvec * VEC;
+  if (blockIdx.x == 0)
+  {
+    for (unsigned long long i = tid; i < head; i += TPB)
+    {
+      fn(keys[i]);
+    }
+    for (unsigned long long i = body_end + tid; i < n; i += TPB)
+    {
+      fn(keys[i]);
+    }
+  }
+  const uint4* vkeys = reinterpret_cast<const uint4*>(keys + head);
+  for (unsigned long long v = blockIdx.x * (unsigned long long) TPB + tid; v < nvec;
+       v += (unsigned long long) gridDim.x * TPB)
+  {
+    const uint4 w = __ldcs(vkeys + v);
+    U k[VEC];
+    memcpy(k, &w, 16);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+    {
+      fn(k[j]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// histogram: counts of every pass's digit in one read; the last CTA writes the exclusive
+// prefix (global digit bases) of portion 0 for every pass. Also clears pass 0's look-back.
+// ---------------------------------------------------------------------------------------
+template <int KB, bool FP, int TPB>
+__device__ __forceinline__ void histogram_body(const HistogramParams& p)
+{
+  using U         = typename uint_of<KB>::type;
+  constexpr int R = RADIX_DIGITS;
+  __shared__ uint32_t sh[MAX_PASSES * R];
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
+
+  const int tid = threadIdx.x;
+  for (int i = tid; i < MAX_PASSES * R; i += TPB)
+  {
+    sh[i] = 0;
+  }
+  __syncthreads();
+
+  int shift[MAX_PASSES];
+  uint32_t mask[MAX_PASSES];
+#pragma unroll
+  for (int q = 0; q < MAX_PASSES; ++q)
+  {
+    const int b  = p.begin_bit + q * RADIX_BITS;
+    const int nb = min(RADIX_BITS, p.end_bit - b);
+    shift[q]     = b;
+    mask[q]      = (q < p.num_passes) ? ((1u << nb) - 1u) : 0u;
+  }
+
+  auto count_key = [&](U raw) {
+    const U t = encode_key<U>(raw, p.codec);
+#pragma unroll
+    for (int q = 0; q < MAX_PASSES; ++q)
+    {
+      if (q < p.num_passes)
+      {
+        atomicAdd(&sh[q * R + extract_digit<U, FP>(t, shift[q], mask[q])], 1u);
+      }
+    }
+  };
+
+  histogram_for_each_key<KB, TPB>(p.keys, p.num_items, count_key);
+  histogram_finish<TPB>(p, sh);
 }
 
 // ---------------------------------------------------------------------------------------

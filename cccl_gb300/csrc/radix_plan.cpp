@@ -36,6 +36,20 @@ RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind)
   return p;
 }
 
+RadixKernelNames radix_kernel_names(int kb, int vb, int kind)
+{
+  const std::string kv = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_" + (kind == KIND_FLOAT ? "f" : "i");
+  RadixKernelNames n;
+  n.init      = "gb300_init";
+  n.histogram = "gb300_histogram_k" + std::to_string(kb) + "_" + (kind == KIND_FLOAT ? "f" : "i");
+  n.onesweep  = "gb300_onesweep_" + kv;
+  n.onesweep_dyn = "gb300_onesweep_dyn_" + kv;
+  // integer keys-only sorts have an order-free first-pass kernel
+  n.onesweep_first = (vb == 0 && kind != KIND_FLOAT) ? "gb300_onesweep_first_" + kv : n.onesweep;
+  n.single_tile    = "gb300_single_tile_" + kv;
+  return n;
+}
+
 static uint64_t ceil_div(uint64_t a, uint64_t b)
 {
   return (a + b - 1) / b;
@@ -133,6 +147,10 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
   }
 
   const KeyCodec codec = make_codec(pol.key_kind, kb, c.descending);
+  if (c.gate.gate != nullptr && (c.begin_bit == c.end_bit || n <= cub_single_tile_limit(kb, vb)))
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "a gated sort must take the onesweep path");
+  }
 
   if (c.begin_bit == c.end_bit)
   {
@@ -204,6 +222,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     InitParams p{};
     p.words     = reinterpret_cast<uint32_t*>(ctrl);
     p.num_words = t.ctrl_bytes / 4;
+    p.gate      = c.gate;
     const unsigned grid = unsigned(std::min<uint64_t>(ceil_div(p.num_words, 256), 1024));
     launch("init", ks.init, grid, 256, 0, c.stream, p);
   }
@@ -221,6 +240,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.bins           = bins;
     p.lookback_clear = lb[0];
     p.lookback_words = t.lookback_words;
+    p.gate           = c.gate;
     const uint64_t want = ceil_div(n, uint64_t(pol.histogram_tpb) * (16 / kb) * 4);
     const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sm_count()) * 4)));
     launch("histogram", ks.histogram, grid, unsigned(pol.histogram_tpb), 0, c.stream, p);
@@ -277,6 +297,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.num_bits      = std::min(RADIX_BITS, c.end_bit - bit);
       op.encode_in     = p == 0;
       op.decode_out    = p == passes - 1;
+      op.gate          = c.gate;
       if (persistent)
       {
         const bool order_free =

@@ -6,6 +6,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 
 #include "sort_params.h"
 
@@ -45,6 +46,13 @@ struct RadixKernels
   CUkernel single_tile;
 };
 
+// Kernel names of one (key width, value width, key kind) in the radix image.
+struct RadixKernelNames
+{
+  std::string init, histogram, onesweep, onesweep_first, onesweep_dyn, single_tile;
+};
+RadixKernelNames radix_kernel_names(int key_bytes, int value_bytes, int key_kind);
+
 struct RadixCall
 {
   void* keys[2];   // [0] = current (input), [1] = alternate (output)
@@ -57,6 +65,7 @@ struct RadixCall
   void* d_temp_storage;
   size_t* temp_storage_bytes;
   CUstream stream;
+  KernelGate gate; // null: always run; else the kernels run only if the flag is set (onesweep path only)
 };
 
 // Byte layout of the temporary storage of one call.

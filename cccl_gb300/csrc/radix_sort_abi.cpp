@@ -33,11 +33,6 @@ bool has_decomposer(const cccl_op_t& op)
   return op.name != nullptr && op.name[0] != '\0';
 }
 
-std::string suffix(int kind)
-{
-  return kind == KIND_FLOAT ? "f" : "i";
-}
-
 void free_names(cccl_device_radix_sort_build_result_t* b)
 {
   for (char** p :
@@ -140,15 +135,13 @@ try
   *pol = make_radix_policy(key_bytes, int(value_size), kind);
   pol->magic = POLICY_MAGIC;
 
-  const std::string s   = suffix(kind);
-  const std::string kv  = "k" + std::to_string(key_bytes) + "_v" + std::to_string(value_size) + "_" + s;
-  const std::string one = "gb300_onesweep_" + kv;
-  const std::string dyn = "gb300_onesweep_dyn_" + kv;
-  // integer keys-only sorts have an order-free first-pass kernel
-  const std::string first = (value_size == 0 && kind != KIND_FLOAT) ? "gb300_onesweep_first_" + kv : one;
-  const std::string st  = "gb300_single_tile_" + kv;
-  const std::string his = "gb300_histogram_k" + std::to_string(key_bytes) + "_" + s;
-  const std::string ini = "gb300_init";
+  const RadixKernelNames names = radix_kernel_names(key_bytes, int(value_size), kind);
+  const std::string& one   = names.onesweep;
+  const std::string& dyn   = names.onesweep_dyn;
+  const std::string& first = names.onesweep_first;
+  const std::string& st    = names.single_tile;
+  const std::string& his   = names.histogram;
+  const std::string& ini   = names.init;
 
   cccl_device_radix_sort_build_result_t r{};
   r.cc                   = cc_major * 10 + cc_minor;

@@ -28,24 +28,6 @@
 namespace gb300
 {
 
-enum : uint32_t
-{
-  SEG_CTR_SMALL = 0,
-  SEG_CTR_MEDIUM,
-  SEG_CTR_BLOCK_S,
-  SEG_CTR_BLOCK_L,
-  SEG_CTR_DEVICE,
-  SEG_CTR_DEVICE_TILES,
-  SEG_CTR_TICKET_SMALL,
-  SEG_CTR_TICKET_MEDIUM,
-  SEG_CTR_TICKET_BLOCK_S,
-  SEG_CTR_TICKET_BLOCK_L,
-  SEG_CTR_TICKET_HIST,
-  SEG_CTR_TICKET_SCAN,
-  SEG_CTR_TICKET_PASS0, // one per device pass
-  SEG_CTR_COUNT = SEG_CTR_TICKET_PASS0 + 16
-};
-
 __device__ __forceinline__ long long load_offset(const void* p, unsigned long long i, int wide)
 {
   return wide ? static_cast<const long long*>(p)[i] : (long long) static_cast<const int*>(p)[i];
@@ -121,6 +103,7 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
       const uint32_t tiles = uint32_t((size + p.device_tile - 1) / p.device_tile);
       const uint32_t idx   = atomicAdd(p.counters + SEG_CTR_DEVICE, 1u);
       const uint32_t base  = atomicAdd(p.counters + SEG_CTR_DEVICE_TILES, tiles);
+      atomicAdd(reinterpret_cast<unsigned long long*>(p.counters + SEG_CTR_DEVICE_ITEMS), (unsigned long long) size);
       if (idx < p.max_device_segments && (unsigned long long) base + tiles <= p.max_tiles)
       {
         p.device_list[idx] = DeviceSegment{(unsigned long long) b, uint32_t(size), base};

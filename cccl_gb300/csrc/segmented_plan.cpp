@@ -10,6 +10,8 @@
 #include "segmented_plan.h"
 
 #include <algorithm>
+#include <cstdio>
+#include <string>
 
 #include "abi_common.h"
 #include "sort_policy.h"
@@ -23,9 +25,28 @@ uint64_t ceil_div(uint64_t a, uint64_t b)
 {
   return (a + b - 1) / b;
 }
-
-constexpr uint32_t SEG_COUNTERS = 32; // counters + status, see segmented_kernels.cuh
 } // namespace
+
+void segmented_kernel_names(int kb, int vb, int kind, char (&names)[SK_COUNT][64])
+{
+  const std::string kv  = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_";
+  const std::string net = kv + (kind == KIND_FLOAT ? "f" : kind == KIND_SIGNED ? "i" : "u");
+  const std::string rad = kv + (kind == KIND_FLOAT ? "f" : "i");
+  const std::string n[SK_COUNT] = {
+    "gb300_init",
+    "gb300_seg_classify",
+    "gb300_seg_small_" + net,
+    "gb300_seg_medium_" + net,
+    "gb300_seg_block_s_" + rad,
+    "gb300_seg_block_l_" + rad,
+    "gb300_seg_hist_k" + std::to_string(kb) + (kind == KIND_FLOAT ? "_f" : "_i"),
+    "gb300_seg_scan",
+    "gb300_seg_pass_" + rad};
+  for (int i = 0; i < SK_COUNT; ++i)
+  {
+    std::snprintf(names[i], sizeof(names[i]), "%s", n[i].c_str());
+  }
+}
 
 SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
 {
@@ -61,7 +82,11 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
 
   // ---- digit passes of the large segments and the buffer that receives the result ----
   const int pass6_count = int(ceil_div(uint64_t(8 * kb), kb > 1 ? 6 : 4)); // CUB's radix passes
-  const int target      = c.overwrite ? (pass6_count & 1) : 1;
+  const int target      = c.target >= 0 ? c.target : c.overwrite ? (pass6_count & 1) : 1;
+  if (c.target >= 0 && !c.overwrite && c.target != 1)
+  {
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "without overwrite the result goes to the output buffer");
+  }
   int bit[SEG_MAX_PASSES];
   int bits[SEG_MAX_PASSES];
   int passes = 0;
@@ -88,7 +113,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
 
   size_t off               = 0;
   const size_t ctrl_off    = off;
-  off += align_up(4 * SEG_COUNTERS, 256);
+  off += align_up(4 * SEG_CTR_WORDS, 256);
   const size_t counts_off  = off;
   off += align_up(4 * size_t(max_dev) * passes * RADIX_DIGITS, 256);
   const size_t zero_bytes  = off; // control block + per-segment counts are zeroed per call
@@ -147,7 +172,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
 
   auto* base     = static_cast<unsigned char*>(c.d_temp_storage);
   auto* counters = reinterpret_cast<uint32_t*>(base + ctrl_off);
-  uint32_t* status = counters + (SEG_COUNTERS - 1);
+  uint32_t* status = counters + SEG_CTR_STATUS;
   auto* lists    = reinterpret_cast<uint32_t*>(base + lists_off);
   const size_t list_stride = align_up(4 * size_t(nseg), 256) / 4;
   auto* dev_list = reinterpret_cast<DeviceSegment*>(base + dev_off);

@@ -56,6 +56,9 @@ struct SegmentedKernels
   CUkernel k[SK_COUNT];
 };
 
+// Kernel names of one (key width, value width, key kind) in the segmented image.
+void segmented_kernel_names(int kb, int vb, int kind, char (&names)[SK_COUNT][64]);
+
 struct SegmentedCall
 {
   void* keys[2];   // [0] = current (input), [1] = alternate (output)
@@ -70,6 +73,7 @@ struct SegmentedCall
   void* d_temp_storage;
   size_t* temp_storage_bytes;
   CUstream stream;
+  int target; // buffer index that receives the result; -1: the one CUB's dispatch picks
 };
 
 // Runs (or sizes, when d_temp_storage is null) one segmented sort; writes the selector

@@ -35,16 +35,6 @@ bool keys_only(const cccl_iterator_t& values)
   return values.type == CCCL_POINTER && values.state == nullptr;
 }
 
-const char* kind_suffix(int kind)
-{
-  return kind == KIND_FLOAT ? "f" : kind == KIND_SIGNED ? "i" : "u";
-}
-
-void set_name(SegKernelTable& t, int i, const std::string& s)
-{
-  std::snprintf(t.names[i], sizeof(t.names[i]), "%s", s.c_str());
-}
-
 void free_result(cccl_device_segmented_sort_build_result_t* b)
 {
   delete[] static_cast<char*>(b->payload);
@@ -123,18 +113,7 @@ try
   *pol       = make_segmented_policy(kb, int(vb), kind);
   pol->magic = SEG_POLICY_MAGIC;
   tab->magic = SEG_TABLE_MAGIC;
-  const std::string kv  = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_";
-  const std::string net = kv + kind_suffix(kind);
-  const std::string rad = kv + (kind == KIND_FLOAT ? "f" : "i");
-  set_name(*tab, SK_INIT, "gb300_init");
-  set_name(*tab, SK_CLASSIFY, "gb300_seg_classify");
-  set_name(*tab, SK_SMALL, "gb300_seg_small_" + net);
-  set_name(*tab, SK_MEDIUM, "gb300_seg_medium_" + net);
-  set_name(*tab, SK_BLOCK_S, "gb300_seg_block_s_" + rad);
-  set_name(*tab, SK_BLOCK_L, "gb300_seg_block_l_" + rad);
-  set_name(*tab, SK_HIST, "gb300_seg_hist_k" + std::to_string(kb) + (kind == KIND_FLOAT ? "_f" : "_i"));
-  set_name(*tab, SK_SCAN, "gb300_seg_scan");
-  set_name(*tab, SK_PASS, "gb300_seg_pass_" + rad);
+  segmented_kernel_names(kb, int(vb), kind, tab->names);
 
   cccl_device_segmented_sort_build_result_t r{};
   r.cc                            = cc_major * 10 + cc_minor;
@@ -345,6 +324,7 @@ CCCL_C_API CUresult cccl_device_segmented_sort(
     call.d_temp_storage     = d_temp_storage;
     call.temp_storage_bytes = temp_storage_bytes;
     call.stream             = stream;
+    call.target             = -1;
     int sel                 = 0;
     segmented_sort_dispatch(pol, ks, call, &sel);
     *selector = sel;

@@ -79,6 +79,12 @@ __device__ __forceinline__ U decode_key(U t, const KeyCodec& c)
 
 // Digit source: for floating-point keys the encoded -0.0 (0x7f..f in both orders) is
 // replaced by the encoded +0.0 pattern (0x80..0) before the shift.
+// False when the kernel is gated off (see KernelGate).
+__device__ __forceinline__ bool gate_open(const KernelGate& g)
+{
+  return g.gate == nullptr || (__ldcg(g.gate) & g.gate_mask) != 0u;
+}
+
 template <class U, bool FP>
 __device__ __forceinline__ U digit_source(U t)
 {

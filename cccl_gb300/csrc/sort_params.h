@@ -39,10 +39,20 @@ struct SortControl
   // followed by tile counters, one per (pass, portion)
 };
 
+// Optional launch gate of the plain-path kernels: with gate non-null a kernel does its
+// work only if (*gate & gate_mask) != 0, a flag an earlier kernel of the same stream set.
+struct KernelGate
+{
+  const uint32_t* gate;
+  uint32_t gate_mask;
+  uint32_t pad0;
+};
+
 struct InitParams
 {
   uint32_t* words;
   unsigned long long num_words;
+  KernelGate gate;
 };
 
 struct HistogramParams
@@ -58,6 +68,7 @@ struct HistogramParams
   unsigned long long* bins;   // [pass][portion][digit], portion 0 written here
   uint32_t* lookback_clear;   // look-back buffer of pass 0, zeroed here
   unsigned long long lookback_words;
+  KernelGate gate;
 };
 
 struct OnesweepParams
@@ -83,6 +94,7 @@ struct OnesweepParams
   int num_bits;
   int encode_in;              // first pass: raw keys are encoded on load
   int decode_out;             // last pass: keys are decoded on store
+  KernelGate gate;
 };
 
 struct SingleTileParams
@@ -100,6 +112,28 @@ struct SingleTileParams
 
 // ---- batched segmented sort ----
 constexpr int SEG_MAX_PASSES = 12; // 8-bit digits, plus one split pass to match CUB's buffer parity
+
+// Counter words at the start of the segmented sort's temporary storage (zeroed per call).
+enum : uint32_t
+{
+  SEG_CTR_SMALL = 0, // segments per class
+  SEG_CTR_MEDIUM,
+  SEG_CTR_BLOCK_S,
+  SEG_CTR_BLOCK_L,
+  SEG_CTR_DEVICE,
+  SEG_CTR_DEVICE_TILES,
+  SEG_CTR_TICKET_SMALL,
+  SEG_CTR_TICKET_MEDIUM,
+  SEG_CTR_TICKET_BLOCK_S,
+  SEG_CTR_TICKET_BLOCK_L,
+  SEG_CTR_TICKET_HIST,
+  SEG_CTR_TICKET_SCAN,
+  SEG_CTR_TICKET_PASS0, // one per device pass
+  SEG_CTR_COUNT        = SEG_CTR_TICKET_PASS0 + 16,
+  SEG_CTR_DEVICE_ITEMS = SEG_CTR_COUNT, // u64 (two words): keys in device-class segments
+  SEG_CTR_STATUS       = 31,
+  SEG_CTR_WORDS        = 32
+};
 
 struct DeviceSegment
 {
@@ -174,6 +208,67 @@ struct SegDeviceParams
   uint32_t* lookback[2];
   uint32_t* status;
   KeyCodec codec;
+};
+
+// ---- learned-partition sort ----
+constexpr int LEARNED_SAMPLE_LOG2 = 16;  // keys in the model's sample
+constexpr int LEARNED_SAMPLE      = 1 << LEARNED_SAMPLE_LOG2;
+constexpr int LEARNED_LEAVES      = 256; // linear pieces of the second level
+constexpr int LEARNED_MAX_BUCKET_LOG2 = 24;
+
+// Two-level piecewise-linear model of the keys' CDF, in sample ranks. Level one: the sorted
+// sample cut into LEARNED_LEAVES leaves of equal sample count, leaf j starting at knot[j]
+// (an encoded key); a key belongs to the last leaf whose knot is <= the key. Level two: a
+// least-squares line per leaf, rank = slope[j] * (key - knot[j]) + icpt[j], slope >= 0,
+// clamped to the leaf's own rank range [j * P, (j + 1) * P] (P = sample / leaves). The
+// predicted rank is therefore non-decreasing in the key, whatever the fit.
+struct LearnedModel
+{
+  unsigned long long knot[LEARNED_LEAVES];
+  float slope[LEARNED_LEAVES];
+  float icpt[LEARNED_LEAVES];
+};
+
+struct LearnedSampleParams
+{
+  const void* keys;
+  unsigned long long num_items;
+  void* sample; // [LEARNED_SAMPLE] encoded keys, -0.0 folded into +0.0
+  KeyCodec codec;
+};
+
+struct LearnedFitParams
+{
+  const void* sorted_sample;
+  LearnedModel* model;
+};
+
+// bucket = floor(rank * 2^bucket_log2 / LEARNED_SAMPLE), in [0, 2^bucket_log2)
+struct LearnedHistParams
+{
+  HistogramParams h; // num_passes = partition passes; digit q = bits [8q, 8q+8) of the bucket
+  const LearnedModel* model;
+  int bucket_log2;
+  int pad0;
+};
+
+struct LearnedPassParams
+{
+  OnesweepParams os;
+  const LearnedModel* model;
+  int bucket_log2;
+  int digit_shift; // this pass's digit = (bucket >> digit_shift) & 255
+};
+
+struct LearnedBoundsParams
+{
+  const void* keys; // partitioned (raw) keys: bucket ids are non-decreasing along them
+  unsigned long long num_items;
+  const LearnedModel* model;
+  unsigned long long* bounds; // [2^bucket_log2 + 1]: first index of every bucket, then n
+  KeyCodec codec;
+  int bucket_log2;
+  int pad0;
 };
 
 } // namespace gb300

@@ -10,6 +10,8 @@
 
 #include <cstddef>
 
+#include "sort_params.h"
+
 #if defined(__CUDACC__)
 #  define GB300_HD __host__ __device__
 #else
@@ -190,4 +192,39 @@ GB300_HD constexpr size_t block_sort_smem(int kb, int tpb, int items)
 {
   return size_t(4) * (tpb / 32) * 256 + 128 + round16(size_t(2) * kb * tpb * items) + size_t(2) * 2 * tpb * items;
 }
+} // namespace gb300
+
+// ---- learned-partition sort ----
+namespace gb300
+{
+// The partition pass is the persistent onesweep pass plus one shared-memory region: the
+// model's tables (knot, slope, intercept per leaf) and the staged digit of every tile slot.
+GB300_HD constexpr size_t learned_extra_bytes(int kb, int vb, int items)
+{
+  return round16(size_t(LEARNED_LEAVES) * (size_t(kb) + 8)) + round16(size_t(persistent_tpb(kb, vb)) * items);
+}
+
+GB300_HD constexpr int learned_items(int kb, int vb)
+{
+  int items = persistent_items_nominal(kb, vb);
+  while (items > 1
+         && (persistent_smem_for(kb, vb, items) + learned_extra_bytes(kb, vb, items)) * PERSISTENT_MINB
+              > size_t(227) * 1024)
+  {
+    --items;
+  }
+  return items;
+}
+
+GB300_HD constexpr size_t learned_pass_smem(int kb, int vb)
+{
+  return persistent_smem_for(kb, vb, learned_items(kb, vb)) + learned_extra_bytes(kb, vb, learned_items(kb, vb));
+}
+
+constexpr int LEARNED_FIT_TPB    = LEARNED_SAMPLE / LEARNED_LEAVES; // one sample point per thread
+constexpr int LEARNED_BOUNDS_TPB = 256;
+// Smallest input the learned path takes; below it the plain radix sort runs.
+constexpr unsigned long long LEARNED_MIN_ITEMS = 1ull << 20;
+// Target keys per bucket: the buckets' block sort holds up to 8192 keys.
+constexpr int LEARNED_BUCKET_ITEMS_LOG2 = 12;
 } // namespace gb300

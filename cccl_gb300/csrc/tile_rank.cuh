@@ -150,6 +150,41 @@ __device__ __forceinline__ void warp_rank_stable(
   }
 }
 
+// The same two steps for digits computed by the caller (dig[i] < 256), used by passes
+// whose digit is not a bit field of the key.
+template <int ITEMS>
+__device__ __forceinline__ void warp_histogram_digits(const uint32_t (&dig)[ITEMS], uint32_t* whist_w)
+{
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    atomicAdd(&whist_w[dig[i]], 1u);
+  }
+}
+
+template <int ITEMS>
+__device__ __forceinline__ void
+warp_rank_stable_digits(const uint32_t (&dig)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w)
+{
+  const int lane    = threadIdx.x & 31;
+  const uint32_t le = lanemask_le();
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t d      = dig[i];
+    const uint32_t peers  = warp_match_digit(d);
+    const int leader      = 31 - __clz(peers);
+    const uint32_t cnt_le = __popc(peers & le);
+    uint32_t base         = 0;
+    if (lane == leader)
+    {
+      base = atomicAdd(&whist_w[d], cnt_le);
+    }
+    base   = __shfl_sync(0xffffffffu, base, leader);
+    pos[i] = base + cnt_le - 1;
+  }
+}
+
 // Order-free tile positions (same digit buckets, arbitrary order inside a bucket).
 template <class U, bool FP, int ITEMS>
 __device__ __forceinline__ void warp_rank_unstable(

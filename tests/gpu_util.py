@@ -57,8 +57,13 @@ def value_tensor(v: np.ndarray) -> torch.Tensor:
     return t
 
 
-def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, overwrite=False, return_temp=False):
-    """Sorts through cccl_device_radix_sort. Returns (keys, values, selector[, temp])."""
+def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, overwrite=False, return_temp=False,
+             method="plain", stats=None):
+    """Sorts through cccl_device_radix_sort (method "plain") or cccl_gb300_learned_sort
+    (method "learned"; `stats`, a dict, receives the run's counters). Returns
+    (keys, values, selector[, temp])."""
+    from cccl_gb300 import make_learned_sort
+
     order = SortOrder.DESCENDING if descending else SortOrder.ASCENDING
     ki = to_dev(keys)
     ko = empty_like_dev(keys)
@@ -72,10 +77,24 @@ def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, ove
         args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
     else:
         args = dict(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo)
-    sorter = make_radix_sort(order=order, **args)
+    sorter = (make_learned_sort if method == "learned" else make_radix_sort)(order=order, **args)
     nbytes = sorter(temp_storage=None, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit, **args)
     temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
+    sel0 = dk.selector if overwrite else None
     sorter(temp_storage=temp, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit, **args)
+    torch.cuda.synchronize()
+    if stats is not None and method == "learned":
+        sel_final = dk.selector if overwrite else None
+        if overwrite:  # counters are read with the buffers as they were when the run started
+            dk.selector = sel0
+            if dv is not None:
+                dv.selector = sel0
+        stats.update(sorter.stats(temp_storage=temp, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit,
+                                  **args))
+        if overwrite:
+            dk.selector = sel_final
+            if dv is not None:
+                dv.selector = sel_final
     torch.cuda.synchronize()
     if overwrite:
         sel = dk.selector

@@ -73,3 +73,35 @@ def finite_floats(dtype, n: int, rng: np.random.Generator) -> np.ndarray:
 def index_values(n: int, dtype=np.uint32) -> np.ndarray:
     """value = original index: makes stability visible in a pairs sort."""
     return np.arange(n, dtype=dtype)
+
+
+# ---- skewed distributions of the learned-partition sort's workloads ----
+def gaussian_mixture(dtype, n: int, rng: np.random.Generator, components: int = 8) -> np.ndarray:
+    """Equal-weight mixture: means U(-1e3, 1e3), sigmas log-uniform in [1e-2, 1e2]."""
+    means = rng.uniform(-1e3, 1e3, size=components)
+    sigmas = 10.0 ** rng.uniform(-2.0, 2.0, size=components)
+    c = rng.integers(0, components, size=n)
+    return (means[c] + sigmas[c] * rng.standard_normal(n)).astype(dtype)
+
+
+def lognormal(dtype, n: int, rng: np.random.Generator, mu: float = 0.0, sigma: float = 2.0) -> np.ndarray:
+    return rng.lognormal(mu, sigma, size=n).astype(dtype)
+
+
+def zipf_values(dtype, n: int, rng: np.random.Generator, s: float = 1.1, distinct: int = 1 << 20) -> np.ndarray:
+    """Zipf(s) ranks over `distinct` values; rank r maps to the r-th of `distinct` seeded
+    uniform values, so frequency is not monotone in the key."""
+    w = np.arange(1, distinct + 1, dtype=np.float64) ** -s
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    ranks = np.searchsorted(cdf, rng.random(n), side="right")
+    ranks = np.minimum(ranks, distinct - 1)
+    table = rng.uniform(0.0, 1e6, size=distinct).astype(dtype)
+    return table[ranks]
+
+
+def half_uniform_mix(dtype, n: int, rng: np.random.Generator, sigma: float = 3.0) -> np.ndarray:
+    """50/50 mix of lognormal(0, sigma) and U(0, 1)."""
+    a = rng.lognormal(0.0, sigma, size=n)
+    b = rng.random(n)
+    return np.where(rng.random(n) < 0.5, a, b).astype(dtype)

@@ -126,3 +126,43 @@ def test_link_ltoir_has_nothing_to_link(lib):
     rc, b = _compile(lib)
     assert lib.cccl_device_radix_sort_link_ltoir(C.byref(b), None, None, 0) == B.CUDA_ERROR_INVALID_VALUE
     lib.cccl_device_radix_sort_cleanup(C.byref(b))
+
+
+def _learned_build(lib, key_type, value_type=None, order=0, cc=(10, 3)):
+    from cccl_gb300 import _bindings as B
+
+    build = B.LearnedSortBuildResult()
+    keys = B.pointer_iterator(0x1000, key_type[0], key_type[1])
+    vals = B.pointer_iterator(0x2000 if value_type else 0, *(value_type or (B.STORAGE, 4)))
+    return lib.cccl_gb300_learned_sort_build(C.byref(build), order, keys, vals, cc[0], cc[1]), build
+
+
+def test_learned_build_rejections(lib):
+    """Argument checks that run before any device work."""
+    from cccl_gb300 import _bindings as B
+
+    assert _learned_build(lib, (B.FLOAT32, 4), cc=(10, 0))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _learned_build(lib, (B.UINT16, 2))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _learned_build(lib, (B.FLOAT16, 2))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _learned_build(lib, (B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _learned_build(lib, (B.FLOAT64, 8), (B.STORAGE, 16))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _learned_build(lib, (B.FLOAT64, 8), order=7)[0] == B.CUDA_ERROR_INVALID_VALUE
+    assert lib.cccl_gb300_learned_sort_cleanup(None) == B.CUDA_ERROR_INVALID_VALUE
+
+
+def test_learned_run_rejects_what_the_plain_run_rejects(lib):
+    from cccl_gb300 import _bindings as B
+
+    b = B.LearnedSortBuildResult()  # never built: every check below comes first
+    it = B.pointer_iterator(0x1000, B.FLOAT32, 4)
+    bad = B.pointer_iterator(0x1000, B.FLOAT32, 4)
+    bad.type = B.ITERATOR
+    nbytes, sel = C.c_size_t(0), C.c_int(-1)
+    r = lib.cccl_gb300_learned_sort(b, None, C.byref(nbytes), bad, it, it, it, B.Op(), 16, 0, 32, False, C.byref(sel), None)
+    assert r == B.CUDA_ERROR_UNKNOWN
+    r = lib.cccl_gb300_learned_sort(b, None, None, it, it, it, it, B.Op(), 16, 0, 32, False, C.byref(sel), None)
+    assert r == B.CUDA_ERROR_INVALID_VALUE
+    op = B.Op()
+    op.name = b"decomposer"
+    r = lib.cccl_gb300_learned_sort(b, None, C.byref(nbytes), it, it, it, it, op, 16, 0, 32, False, C.byref(sel), None)
+    assert r == B.CUDA_ERROR_NOT_SUPPORTED
