@@ -47,4 +47,8 @@ extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitPa
     const gb300::LearnedFitParams p)                                                                            \
   {                                                                                                             \
     gb300::learned_fit_body<KB>(p);                                                                             \
+  }                                                                                                             \
+  extern "C" __global__ void __launch_bounds__(256) gb300_learned_cells_k##KB(const gb300::LearnedFitParams p)  \
+  {                                                                                                             \
+    gb300::learned_cells_body<KB>(p);                                                                           \
   }

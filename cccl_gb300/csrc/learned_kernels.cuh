@@ -23,11 +23,21 @@ namespace gb300
 {
 
 template <class U>
+struct alignas(16) LearnedLeaf
+{
+  U knot;
+  float slope;
+  float icpt;
+};
+
+// Shared-memory copy of the model (layout size: learned_tables_bytes()).
+template <class U>
 struct LearnedTables
 {
-  U knot[LEARNED_LEAVES];
-  float slope[LEARNED_LEAVES];
-  float icpt[LEARNED_LEAVES];
+  LearnedLeaf<U> leaf[LEARNED_LEAVES];
+  unsigned char cell_leaf[LEARNED_CELLS + 16];
+  U kmin;
+  int shift;
 };
 
 template <class U>
@@ -35,9 +45,20 @@ __device__ __forceinline__ void learned_load_tables(const LearnedModel* m, Learn
 {
   for (int i = threadIdx.x; i < LEARNED_LEAVES; i += blockDim.x)
   {
-    t->knot[i]  = U(m->knot[i]);
-    t->slope[i] = m->slope[i];
-    t->icpt[i]  = m->icpt[i];
+    t->leaf[i].knot  = U(m->knot[i]);
+    t->leaf[i].slope = m->slope[i];
+    t->leaf[i].icpt  = m->icpt[i];
+  }
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(m->cell_leaf);
+  uint32_t* dst       = reinterpret_cast<uint32_t*>(t->cell_leaf);
+  for (int i = threadIdx.x; i < (LEARNED_CELLS + 16) / 4; i += blockDim.x)
+  {
+    dst[i] = src[i];
+  }
+  if (threadIdx.x == 0)
+  {
+    t->kmin  = U(m->kmin);
+    t->shift = m->shift;
   }
 }
 
@@ -51,7 +72,33 @@ __device__ __forceinline__ float learned_to_float(unsigned long long x)
   return __ull2float_rn(x);
 }
 
-// Bucket of an encoded key. Every step is non-decreasing in the key: the leaf search, the
+// Leaf of an encoded key: the last leaf whose knot is <= the key, searched only among the
+// leaves of the key's cell (the first leaf if no knot is <= the key).
+template <class U>
+__device__ __forceinline__ int learned_leaf(U k, const LearnedTables<U>& t)
+{
+  const U d        = k > t.kmin ? U(k - t.kmin) : U(0);
+  const U c_wide   = d >> t.shift;
+  const uint32_t c = c_wide < U(LEARNED_CELLS - 1) ? uint32_t(c_wide) : uint32_t(LEARNED_CELLS - 1);
+  int j            = t.cell_leaf[c];
+  int span         = int(t.cell_leaf[c + 1]) - j;
+  while (span > 0)
+  {
+    const int half = (span + 1) >> 1;
+    if (t.leaf[j + half].knot <= k)
+    {
+      j += half;
+      span -= half;
+    }
+    else
+    {
+      span = half - 1;
+    }
+  }
+  return j;
+}
+
+// Bucket of an encoded key. Every step is non-decreasing in the key: the leaf lookup, the
 // conversion of (key - knot) to float, the fused multiply-add with a slope >= 0, the clamp
 // to the leaf's rank range (leaf j's top equals leaf j+1's bottom) and the truncation after
 // scaling by a power of two.
@@ -59,23 +106,15 @@ template <class U, bool FP>
 __device__ __forceinline__ uint32_t
 learned_bucket(U enc, const LearnedTables<U>& t, float scale, uint32_t bmax)
 {
-  const U k = digit_source<U, FP>(enc);
-  int j     = 0;
-#pragma unroll
-  for (int s = LEARNED_LEAVES / 2; s >= 1; s >>= 1)
-  {
-    if (t.knot[j + s] <= k)
-    {
-      j += s;
-    }
-  }
-  const U kn             = t.knot[j];
-  const float x          = k > kn ? learned_to_float(k - kn) : 0.0f;
-  constexpr float span   = float(LEARNED_SAMPLE / LEARNED_LEAVES);
-  const float lo         = float(j) * span;
-  float r                = fmaf(t.slope[j], x, t.icpt[j]);
-  r                      = fminf(fmaxf(r, lo), lo + span);
-  const uint32_t b       = uint32_t(r * scale);
+  const U k                = digit_source<U, FP>(enc);
+  const int j              = learned_leaf<U>(k, t);
+  const LearnedLeaf<U> lf  = t.leaf[j];
+  const float x            = k > lf.knot ? learned_to_float(U(k - lf.knot)) : 0.0f;
+  constexpr float span     = float(LEARNED_SAMPLE / LEARNED_LEAVES);
+  const float lo           = float(j) * span;
+  float r                  = fmaf(lf.slope, x, lf.icpt);
+  r                        = fminf(fmaxf(r, lo), lo + span);
+  const uint32_t b         = uint32_t(r * scale);
   return b < bmax ? b : bmax;
 }
 
@@ -181,6 +220,45 @@ __device__ __forceinline__ void learned_fit_body(const LearnedFitParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
+// cells: thread c finds the leaf of cell c's lowest key (c = LEARNED_CELLS: of the largest
+// key); thread 0 also stores kmin and the cell width
+// ---------------------------------------------------------------------------------------
+template <int KB>
+__device__ __forceinline__ void learned_cells_body(const LearnedFitParams& p)
+{
+  using U          = typename uint_of<KB>::type;
+  const U* s       = static_cast<const U*>(p.sorted_sample);
+  const U kmin     = s[0];
+  const U width    = U(s[LEARNED_SAMPLE - 1] - kmin);
+  const int bits   = width == 0 ? 0 : (KB == 8 ? 64 - __clzll((long long) width) : 32 - __clz(uint32_t(width)));
+  const int shift  = bits > LEARNED_CELLS_LOG2 ? bits - LEARNED_CELLS_LOG2 : 0;
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c == 0)
+  {
+    p.model->kmin  = (unsigned long long) kmin;
+    p.model->shift = shift;
+  }
+  if (c > uint32_t(LEARNED_CELLS))
+  {
+    return;
+  }
+  // lowest key of the cell, saturated at the top of the key range
+  const U off    = U(c) << shift;
+  const bool sat = (shift >= 8 * KB) || ((U(c) << shift) >> shift) != U(c) || U(kmin + off) < kmin;
+  const U lo_key = sat ? U(~U(0)) : U(kmin + off);
+  int j          = 0;
+#pragma unroll 1
+  for (int st = LEARNED_LEAVES / 2; st >= 1; st >>= 1)
+  {
+    if (U(p.model->knot[j + st]) <= lo_key)
+    {
+      j += st;
+    }
+  }
+  p.model->cell_leaf[c] = (unsigned char) j;
+}
+
+// ---------------------------------------------------------------------------------------
 // hist: digit counts of every partition pass in one read of the keys
 // ---------------------------------------------------------------------------------------
 template <int KB, bool FP, int TPB>
@@ -230,7 +308,8 @@ struct LearnedPassHook
   template <int ITEMS>
   using digits_t = ComputedDigits<ITEMS>;
 
-  static constexpr size_t tables_bytes = round16(sizeof(LearnedTables<U>));
+  static constexpr size_t tables_bytes = learned_tables_bytes();
+  static_assert(sizeof(LearnedTables<U>) <= learned_tables_bytes(), "learned tables layout");
 
   __device__ __forceinline__ void setup(unsigned char* extra) const
   {
@@ -259,8 +338,6 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
   constexpr int TPB   = persistent_tpb(KB, VB);
   constexpr int ITEMS = learned_items(KB, VB);
   constexpr size_t EXTRA = learned_extra_bytes(KB, VB, ITEMS);
-  static_assert(LearnedPassHook<U, FP>::tables_bytes == round16(size_t(LEARNED_LEAVES) * (KB + 8)),
-                "learned tables layout");
   const LearnedPassHook<U, FP> hook{p.model, learned_scale(p.bucket_log2), (1u << p.bucket_log2) - 1u, p.digit_shift};
   onesweep_persistent_body<KB, VB, FP, TPB, ITEMS, true, LearnedPassHook<U, FP>, EXTRA>(p.os, hook);
 }

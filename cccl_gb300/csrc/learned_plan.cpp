@@ -195,7 +195,8 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     launch("learned_init", s.lk.init, unsigned(std::min<uint64_t>(ceil_div(p.num_words, 256), 1024)), 256, 0,
            c.stream, p);
   }
-  // 2. sample, 3. its plain radix sort (exact ranks), 4. least-squares fit per leaf
+  // 2. sample, 3. its plain radix sort (exact ranks), 4. least-squares fit per leaf and the
+  // cell table of the leaf lookup
   {
     LearnedSampleParams p{};
     p.keys      = c.keys[0];
@@ -225,6 +226,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     p.sorted_sample = sample[ssel];
     p.model         = model;
     launch("learned_fit", s.lk.fit, unsigned(LEARNED_LEAVES), unsigned(LEARNED_FIT_TPB), 0, c.stream, p);
+    launch("learned_cells", s.lk.cells, unsigned(ceil_div(LEARNED_CELLS + 1, 256)), 256, 0, c.stream, p);
   }
   // 5. digit counts of every partition pass (and pass 0's look-back cleared)
   {

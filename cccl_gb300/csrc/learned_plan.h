@@ -21,6 +21,7 @@ struct LearnedKernels
   CUkernel init;
   CUkernel sample;
   CUkernel fit;
+  CUkernel cells;
   CUkernel hist;
   CUkernel pass;
   CUkernel bounds;

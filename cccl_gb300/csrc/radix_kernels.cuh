@@ -259,16 +259,63 @@ __device__ __forceinline__ void block_sort_body(
   const U* kin     = static_cast<const U*>(keys_in);
 
   __syncthreads();
+  U kor = U(0), kand = U(~U(0)); // over the real keys' digit sources
   for (int s = tid; s < TILE; s += TPB)
   {
-    kbuf[s] = (uint32_t(s) < n) ? encode_key<U>(kin[s], codec) : U(~U(0));
+    U k = U(~U(0));
+    if (uint32_t(s) < n)
+    {
+      k               = encode_key<U>(kin[s], codec);
+      const U src_bits = digit_source<U, FP>(k);
+      kor |= src_bits;
+      kand &= src_bits;
+    }
+    kbuf[s] = k;
     ibuf[s] = uint16_t(s);
   }
 
-  int cur = 0;
-  for (int bit = begin_bit; bit < end_bit; bit += RADIX_BITS)
+  // Only bits that differ between two keys need a pass: a digit equal for every key gives
+  // the identity permutation. Per-warp OR/AND go through whist before its first use.
   {
-    const uint32_t dmask = (1u << min(RADIX_BITS, end_bit - bit)) - 1u;
+    uint32_t v[4] = {uint32_t(kor), uint32_t((unsigned long long) kor >> 32), uint32_t(kand),
+                     uint32_t((unsigned long long) kand >> 32)};
+    v[0] = __reduce_or_sync(0xffffffffu, v[0]);
+    v[1] = __reduce_or_sync(0xffffffffu, v[1]);
+    v[2] = __reduce_and_sync(0xffffffffu, v[2]);
+    v[3] = __reduce_and_sync(0xffffffffu, v[3]);
+    if (lane == 0)
+    {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        whist[warp * 4 + j] = v[j];
+      }
+    }
+  }
+  __syncthreads();
+  unsigned long long vary = 0;
+  {
+    unsigned long long o = 0, a = ~0ull;
+#pragma unroll 1
+    for (int w = 0; w < NW; ++w)
+    {
+      o |= (unsigned long long) whist[w * 4] | ((unsigned long long) whist[w * 4 + 1] << 32);
+      a &= (unsigned long long) whist[w * 4 + 2] | ((unsigned long long) whist[w * 4 + 3] << 32);
+    }
+    const unsigned long long window =
+      (end_bit >= 64 ? ~0ull : ((1ull << end_bit) - 1ull)) & ~((1ull << begin_bit) - 1ull);
+    vary = (o ^ a) & window & (sizeof(U) == 8 ? ~0ull : 0xffffffffull);
+  }
+  __syncthreads(); // whist is zeroed by the first pass
+  const int lo_bit = vary == 0 ? 0 : __ffsll((long long) vary) - 1;
+  const int hi_bit = vary == 0 ? 0 : 64 - __clzll((long long) vary);
+  // warps whose keys are all padding keep them in place: they rank after every real key
+  const int active_warps = int((n + ITEMS * 32 - 1) / (ITEMS * 32));
+
+  int cur = 0;
+  for (int bit = lo_bit; bit < hi_bit; bit += RADIX_BITS)
+  {
+    const uint32_t dmask = (1u << min(RADIX_BITS, hi_bit - bit)) - 1u;
     for (int i = tid; i < NW * R; i += TPB)
     {
       whist[i] = 0;
@@ -281,13 +328,17 @@ __device__ __forceinline__ void block_sort_body(
     uint16_t* id       = ibuf + (cur ^ 1) * TILE;
     const int wofs     = warp * ITEMS * 32 + lane;
 
+    const bool active = warp < active_warps;
     U keys[ITEMS];
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
+    if (active)
     {
-      keys[i] = src[wofs + i * 32];
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        keys[i] = src[wofs + i * 32];
+      }
+      warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
     }
-    warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
     __syncthreads();
     if (tid < R)
     {
@@ -295,13 +346,17 @@ __device__ __forceinline__ void block_sort_body(
       block_digit_offsets<NW>(whist, misc + 8, &tstart);
     }
     __syncthreads();
-    uint32_t pos[ITEMS];
-    warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
+    if (active)
     {
-      dst[pos[i]] = keys[i];
-      id[pos[i]]  = is[wofs + i * 32];
+      uint32_t pos[ITEMS];
+      __syncwarp(); // the warp votes below need a converged warp
+      warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        dst[pos[i]] = keys[i];
+        id[pos[i]]  = is[wofs + i * 32];
+      }
     }
     __syncthreads();
     cur ^= 1;

@@ -222,11 +222,22 @@ constexpr int LEARNED_MAX_BUCKET_LOG2 = 24;
 // least-squares line per leaf, rank = slope[j] * (key - knot[j]) + icpt[j], slope >= 0,
 // clamped to the leaf's own rank range [j * P, (j + 1) * P] (P = sample / leaves). The
 // predicted rank is therefore non-decreasing in the key, whatever the fit.
+// Leaf lookup in O(1): the key range [kmin, kmin + LEARNED_CELLS << shift) is cut into
+// equal cells; cell_leaf[c] is the leaf of the cell's lowest key, so a key of cell c lies
+// in a leaf of [cell_leaf[c], cell_leaf[c + 1]] (a short search only where a cell holds
+// several leaves, i.e. where the keys are dense).
+constexpr int LEARNED_CELLS_LOG2 = 12;
+constexpr int LEARNED_CELLS      = 1 << LEARNED_CELLS_LOG2;
+
 struct LearnedModel
 {
   unsigned long long knot[LEARNED_LEAVES];
   float slope[LEARNED_LEAVES];
   float icpt[LEARNED_LEAVES];
+  unsigned long long kmin;
+  int shift;
+  int pad0;
+  unsigned char cell_leaf[LEARNED_CELLS + 16]; // [LEARNED_CELLS + 1] used
 };
 
 struct LearnedSampleParams
@@ -242,6 +253,7 @@ struct LearnedFitParams
   const void* sorted_sample;
   LearnedModel* model;
 };
+// the cell table (one thread per cell) runs after the fit with the same parameters
 
 // bucket = floor(rank * 2^bucket_log2 / LEARNED_SAMPLE), in [0, 2^bucket_log2)
 struct LearnedHistParams

@@ -199,9 +199,15 @@ namespace gb300
 {
 // The partition pass is the persistent onesweep pass plus one shared-memory region: the
 // model's tables (knot, slope, intercept per leaf) and the staged digit of every tile slot.
+// Shared-memory copy of the model: 16-byte leaves, the cell table, kmin and shift.
+GB300_HD constexpr size_t learned_tables_bytes()
+{
+  return size_t(16) * LEARNED_LEAVES + round16(size_t(LEARNED_CELLS) + 16) + 16;
+}
+
 GB300_HD constexpr size_t learned_extra_bytes(int kb, int vb, int items)
 {
-  return round16(size_t(LEARNED_LEAVES) * (size_t(kb) + 8)) + round16(size_t(persistent_tpb(kb, vb)) * items);
+  return (void) kb, learned_tables_bytes() + round16(size_t(persistent_tpb(kb, vb)) * items);
 }
 
 GB300_HD constexpr int learned_items(int kb, int vb)
