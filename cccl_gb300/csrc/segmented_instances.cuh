@@ -41,16 +41,20 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
 
 // radix kernels (integer kinds share them: the order lives in the runtime key codec)
 #define GB300_SEG_RADIX(KB, FP, FS, VB)                                                                              \
-  extern "C" __global__ void __launch_bounds__(gb300::SEG_BLOCK_S_TPB)                                               \
+  static_assert(gb300::seg_block_algo(KB) != gb300::SEG_BLOCK_MERGE                                                  \
+                  || gb300::BlockMergeSmem<KB, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)>::bytes      \
+                       == gb300::block_merge_smem(KB, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)),     \
+                "block merge shared-memory layout");                                                                 \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_block_s_tpb(KB), gb300::seg_block_minb(KB))              \
     gb300_seg_block_s_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                             \
   {                                                                                                                  \
-    gb300::seg_block_body<KB, VB, FP, gb300::SEG_BLOCK_S_TPB, gb300::SEG_BLOCK_S_ITEMS>(                             \
+    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_s_tpb(KB), gb300::seg_block_s_items(KB)>(                     \
       p, p.block_s_list, gb300::SEG_CTR_BLOCK_S, gb300::SEG_CTR_TICKET_BLOCK_S);                                     \
   }                                                                                                                  \
-  extern "C" __global__ void __launch_bounds__(gb300::SEG_BLOCK_L_TPB)                                               \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_block_l_tpb(KB), gb300::seg_block_minb(KB))              \
     gb300_seg_block_l_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                             \
   {                                                                                                                  \
-    gb300::seg_block_body<KB, VB, FP, gb300::SEG_BLOCK_L_TPB, gb300::SEG_BLOCK_L_ITEMS>(                             \
+    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)>(                     \
       p, p.block_l_list, gb300::SEG_CTR_BLOCK_L, gb300::SEG_CTR_TICKET_BLOCK_L);                                     \
   }                                                                                                                  \
   extern "C" __global__ void __launch_bounds__(gb300::SEG_PASS_TPB)                                                  \

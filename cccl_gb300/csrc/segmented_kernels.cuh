@@ -22,6 +22,7 @@
 
 #include <cuda_fp16.h>
 
+#include "block_merge.cuh"
 #include "onesweep.cuh"
 #include "radix_kernels.cuh"
 
@@ -528,14 +529,26 @@ __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uin
     const uint32_t s  = list[item];
     const long long b = load_offset(p.begin_offsets, s, p.offsets_64);
     const uint32_t n  = uint32_t(load_offset(p.end_offsets, s, p.offsets_64) - b);
-    block_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
-                                            static_cast<U*>(p.keys_out) + b,
-                                            VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
-                                            VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
-                                            n,
-                                            0,
-                                            8 * KB,
-                                            p.codec);
+    if constexpr (seg_block_algo(KB) == SEG_BLOCK_MERGE)
+    {
+      block_merge_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
+                                                    static_cast<U*>(p.keys_out) + b,
+                                                    VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
+                                                    VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
+                                                    n,
+                                                    p.codec);
+    }
+    else
+    {
+      block_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
+                                              static_cast<U*>(p.keys_out) + b,
+                                              VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
+                                              VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
+                                              n,
+                                              0,
+                                              8 * KB,
+                                              p.codec);
+    }
   }
 }
 

@@ -58,14 +58,16 @@ SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
   p.small_items         = seg_small_items(kb, vb);
   p.medium_threads      = seg_medium_threads(kb, vb);
   p.medium_items        = seg_medium_items(kb, vb);
-  p.block_s_cap         = SEG_BLOCK_S_TPB * SEG_BLOCK_S_ITEMS;
-  p.block_l_cap         = SEG_BLOCK_L_TPB * SEG_BLOCK_L_ITEMS;
+  p.block_s_cap         = SEG_BLOCK_S_CAP;
+  p.block_l_cap         = SEG_BLOCK_L_CAP;
   p.pass_tpb            = SEG_PASS_TPB;
   p.pass_items          = onesweep_items(kb, vb);
   p.network_small_smem  = seg_network_smem(kb, vb, p.small_threads, p.small_items);
   p.network_medium_smem = seg_network_smem(kb, vb, p.medium_threads, p.medium_items);
-  p.block_s_smem        = block_sort_smem(kb, SEG_BLOCK_S_TPB, SEG_BLOCK_S_ITEMS);
-  p.block_l_smem        = block_sort_smem(kb, SEG_BLOCK_L_TPB, SEG_BLOCK_L_ITEMS);
+  p.block_s_tpb         = seg_block_s_tpb(kb);
+  p.block_l_tpb         = seg_block_l_tpb(kb);
+  p.block_s_smem        = seg_block_smem(kb, seg_block_s_tpb(kb), seg_block_s_items(kb));
+  p.block_l_smem        = seg_block_smem(kb, seg_block_l_tpb(kb), seg_block_l_items(kb));
   p.pass_smem           = onesweep_smem_bytes(kb, vb);
   return p;
 }
@@ -248,10 +250,10 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     launch("seg_medium", ks.k[SK_MEDIUM],
            unsigned(sms * occupancy(ks.k[SK_MEDIUM], SEG_NETWORK_TPB, pol.network_medium_smem)), SEG_NETWORK_TPB,
            pol.network_medium_smem, c.stream, p);
-    launch("seg_block_s", ks.k[SK_BLOCK_S], unsigned(sms * occupancy(ks.k[SK_BLOCK_S], SEG_BLOCK_S_TPB, pol.block_s_smem)),
-           SEG_BLOCK_S_TPB, pol.block_s_smem, c.stream, p);
-    launch("seg_block_l", ks.k[SK_BLOCK_L], unsigned(sms * occupancy(ks.k[SK_BLOCK_L], SEG_BLOCK_L_TPB, pol.block_l_smem)),
-           SEG_BLOCK_L_TPB, pol.block_l_smem, c.stream, p);
+    launch("seg_block_s", ks.k[SK_BLOCK_S], unsigned(sms * occupancy(ks.k[SK_BLOCK_S], pol.block_s_tpb, pol.block_s_smem)),
+           unsigned(pol.block_s_tpb), pol.block_s_smem, c.stream, p);
+    launch("seg_block_l", ks.k[SK_BLOCK_L], unsigned(sms * occupancy(ks.k[SK_BLOCK_L], pol.block_l_tpb, pol.block_l_smem)),
+           unsigned(pol.block_l_tpb), pol.block_l_smem, c.stream, p);
   }
   // 4. device class: every large segment together, one launch per digit pass
   if (max_dev > 0)

@@ -25,6 +25,8 @@ struct SegmentedPolicy
   int32_t medium_items;
   int32_t block_s_cap;
   int32_t block_l_cap;
+  int32_t block_s_tpb;
+  int32_t block_l_tpb;
   int32_t pass_tpb;
   int32_t pass_items;
   uint64_t network_small_smem;

@@ -172,11 +172,53 @@ GB300_HD constexpr int seg_medium_items(int kb, int vb)
 }
 constexpr int SEG_PARTITION_THRESHOLD = 500; // dispatch_segmented_sort.cuh:465
 
-// Block classes (tuned here, free of the reference): one CTA, shared-memory passes.
-constexpr int SEG_BLOCK_S_TPB   = 256;
-constexpr int SEG_BLOCK_S_ITEMS = 8;  // <= 2048 keys
-constexpr int SEG_BLOCK_L_TPB   = 512;
-constexpr int SEG_BLOCK_L_ITEMS = 16; // <= 8192 keys
+// Block classes (free of the reference): one CTA sorts one segment in shared memory, by a
+// stable merge sort or by LSD radix passes; the algorithm and shape per key width come from
+// measurements on GB300 (the GB300_SEG_BLOCK_* macros override them in tuning builds).
+// Measured (2^28 keys in ~4096-key segments, block_l time): 4-byte keys radix 512x16 4.57 ms,
+// with 2 CTAs/SM 3.40 ms, 1024x8 4.41 ms, merge 11.4 ms; 8-byte keys radix 512x16 10.4 ms,
+// 2 CTAs/SM 14.2 ms, 1024x8 10.1 ms, merge 14.2 ms.
+constexpr int SEG_BLOCK_S_CAP = 2048;
+constexpr int SEG_BLOCK_L_CAP = 8192;
+constexpr int SEG_BLOCK_RADIX = 0;
+constexpr int SEG_BLOCK_MERGE = 1;
+GB300_HD constexpr int seg_block_algo(int kb)
+{
+#ifdef GB300_SEG_BLOCK_ALGO
+  return (void) kb, GB300_SEG_BLOCK_ALGO;
+#else
+  return (void) kb, SEG_BLOCK_RADIX; // measured: radix beats merge for 4- and 8-byte keys too
+#endif
+}
+// CTAs per SM the block-class registers are sized for
+GB300_HD constexpr int seg_block_minb(int kb)
+{
+#ifdef GB300_SEG_BLOCK_MINB
+  return (void) kb, GB300_SEG_BLOCK_MINB;
+#else
+  return kb == 4 ? 2 : 1;
+#endif
+}
+GB300_HD constexpr int seg_block_s_items(int kb)
+{
+  return (void) kb, 8;
+}
+GB300_HD constexpr int seg_block_l_items(int kb)
+{
+#ifdef GB300_SEG_BLOCK_L_ITEMS
+  return (void) kb, GB300_SEG_BLOCK_L_ITEMS;
+#else
+  return seg_block_algo(kb) == SEG_BLOCK_MERGE || kb == 8 ? 8 : 16;
+#endif
+}
+GB300_HD constexpr int seg_block_s_tpb(int kb)
+{
+  return SEG_BLOCK_S_CAP / seg_block_s_items(kb);
+}
+GB300_HD constexpr int seg_block_l_tpb(int kb)
+{
+  return SEG_BLOCK_L_CAP / seg_block_l_items(kb);
+}
 constexpr int SEG_NETWORK_TPB   = 256;
 constexpr int SEG_PASS_TPB      = ONESWEEP_TPB;
 } // namespace gb300
@@ -191,6 +233,15 @@ GB300_HD constexpr size_t seg_network_smem(int kb, int vb, int threads, int item
 GB300_HD constexpr size_t block_sort_smem(int kb, int tpb, int items)
 {
   return size_t(4) * (tpb / 32) * 256 + 128 + round16(size_t(2) * kb * tpb * items) + size_t(2) * 2 * tpb * items;
+}
+GB300_HD constexpr size_t block_merge_smem(int kb, int tpb, int items)
+{
+  return round16(size_t(kb) * (size_t(tpb) * items + size_t(tpb) * items / (kb == 8 ? 16 : 32) + 1))
+       + round16(size_t(2) * (size_t(tpb) * items + 2 * (size_t(tpb) * items / 64) + 2));
+}
+GB300_HD constexpr size_t seg_block_smem(int kb, int tpb, int items)
+{
+  return seg_block_algo(kb) == SEG_BLOCK_MERGE ? block_merge_smem(kb, tpb, items) : block_sort_smem(kb, tpb, items);
 }
 } // namespace gb300
 
