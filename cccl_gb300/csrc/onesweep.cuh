@@ -44,7 +44,8 @@ struct OnesweepSmem
   static constexpr size_t bytes      = vstage_off + (VB > 0 ? sizeof(V) * TILE : 0);
 };
 // misc words: [0] tile id, [1] tile failed (stores disabled), [2] sticky failure of the
-// CTA, [8..15] scan scratch, [16..19] two mbarriers (persistent kernel).
+// CTA, [3] single-digit tile flag and digit, [8..15] scan scratch, [16..19] two mbarriers
+// (persistent kernel).
 
 // Where a pass takes its digits from.
 //   RadixDigits: bits [current_bit, current_bit + num_bits) of the encoded key, recomputed
@@ -110,6 +111,35 @@ __device__ __forceinline__ void onesweep_tile(
   // ---- tile positions; publish the tile's digit counts; look-back ----
   if (tid < R)
   {
+    if (STABLE && tid < 32)
+    {
+      // Short circuit (the reference's TryShortCircuit, agent_radix_sort_onesweep.cuh:386-467):
+      // when every real key of the tile has the tile's first digit, the stable permutation is
+      // the identity and the keys go out straight from registers. misc[3] = flag | digit << 8;
+      // the barrier inside block_digit_offsets publishes it to warps 0-7, bar 2 to the rest.
+      uint32_t d0;
+      if constexpr (Digits::computed)
+      {
+        d0 = dg.d[0];
+      }
+      else
+      {
+        d0 = extract_digit<U, FP>(keys[0], bit, dmask);
+      }
+      d0         = __shfl_sync(0xffffffffu, d0, 0);
+      uint32_t c = 0;
+      for (int w = tid; w < NW; w += 32)
+      {
+        c += whist[w * R + d0];
+      }
+      c = __reduce_add_sync(0xffffffffu, c);
+      const uint32_t pad_digit = Digits::computed ? 255u : dmask;
+      const uint32_t real_d0   = c - (d0 == pad_digit ? uint32_t(TILE) - valid : 0u);
+      if (tid == 0)
+      {
+        misc[3] = real_d0 == valid ? (1u | (d0 << 8)) : 0u;
+      }
+    }
     uint32_t start;
     const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start);
     uint32_t* lb_row     = p.lookback + (size_t) (p.tile_row_base + tile) * R;
@@ -179,75 +209,112 @@ __device__ __forceinline__ void onesweep_tile(
     asm volatile("bar.sync 2, %0;" ::"n"(TPB) : "memory");
   }
 
-  // ---- stable ranks, scatter into the staging tile ----
-  uint32_t pos[ITEMS];
-  __syncwarp(); // reconverge after the divergent look-back before the warp votes
-  if constexpr (Digits::computed)
+  // (not in the order-free first-pass kernel: ptxas cannot allocate its ballot loop with the
+  // extra branch, and that kernel sorts integer keys only, where single-digit tiles are rare)
+  const uint32_t single = STABLE ? misc[3] : 0u;
+  const unsigned long long out_limit_early = p.num_items_total;
+  U* kout                                  = static_cast<U*>(p.keys_out);
+  V* vout                                  = static_cast<V*>(p.values_out);
+  if (single != 0u)
   {
-    warp_rank_stable_digits<ITEMS>(dg.d, pos, whist + warp * R);
-  }
-  else if (STABLE || !full) // a partial tile's padding keys must rank after its real keys
-  {
-    warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+    // ---- one digit: tile order is the output order ----
+    V vals[VB > 0 ? ITEMS : 1];
+    if constexpr (VB > 0)
+    {
+      load_values(vals);
+    }
+    __syncthreads(); // gdelta written; misc[1] final
+    const unsigned long long out_limit = misc[1] != 0u ? 0ull : out_limit_early;
+    const long long base               = gdelta[single >> 8];
+    const uint32_t wofs                = uint32_t(warp * ITEMS * 32 + (tid & 31));
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i)
+    {
+      const uint32_t s = wofs + i * 32;
+      if (full || s < valid)
+      {
+        const long long g = base + (long long) s;
+        if ((unsigned long long) g < out_limit)
+        {
+          __stcs(kout + g, p.decode_out ? decode_key<U>(keys[i], p.codec) : keys[i]);
+          if constexpr (VB > 0)
+          {
+            __stcs(vout + g, vals[i]);
+          }
+        }
+      }
+    }
   }
   else
   {
-    warp_rank_unstable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
-  }
-#pragma unroll
-  for (int i = 0; i < ITEMS; ++i)
-  {
-    kstage[pos[i]] = keys[i];
-  }
-  if constexpr (Digits::computed)
-  {
+    // ---- stable ranks, scatter into the staging tile ----
+    uint32_t pos[ITEMS];
+    __syncwarp(); // reconverge after the divergent look-back before the warp votes
+    if constexpr (Digits::computed)
+    {
+      warp_rank_stable_digits<ITEMS>(dg.d, pos, whist + warp * R);
+    }
+    else if (STABLE || !full) // a partial tile's padding keys must rank after its real keys
+    {
+      warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+    }
+    else
+    {
+      warp_rank_unstable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+    }
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i)
     {
-      dg.stage[pos[i]] = uint8_t(dg.d[i]);
+      kstage[pos[i]] = keys[i];
     }
-  }
-  if constexpr (VB > 0)
-  {
-    V vals[ITEMS];
-    load_values(vals);
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i)
+    if constexpr (Digits::computed)
     {
-      vstage[pos[i]] = vals[i];
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        dg.stage[pos[i]] = uint8_t(dg.d[i]);
+      }
     }
-  }
-  __syncthreads();
+    if constexpr (VB > 0)
+    {
+      V vals[ITEMS];
+      load_values(vals);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        vstage[pos[i]] = vals[i];
+      }
+    }
+    __syncthreads();
 
-  // ---- write out: consecutive staging slots of one digit go to consecutive outputs.
-  // Every store is bounds-checked against the output size, so even corrupted offsets
-  // (a look-back that gave up) cannot write outside the caller's buffers.
-  const unsigned long long out_limit = misc[1] != 0u ? 0ull : p.num_items_total;
-  U* kout                            = static_cast<U*>(p.keys_out);
-  V* vout                            = static_cast<V*>(p.values_out);
+    // ---- write out: consecutive staging slots of one digit go to consecutive outputs.
+    // Every store is bounds-checked against the output size, so even corrupted offsets
+    // (a look-back that gave up) cannot write outside the caller's buffers.
+    const unsigned long long out_limit = misc[1] != 0u ? 0ull : out_limit_early;
 #pragma unroll
-  for (int j = 0; j < ITEMS; ++j)
-  {
-    const uint32_t s = j * TPB + threadIdx.x;
-    if (full || s < valid)
+    for (int j = 0; j < ITEMS; ++j)
     {
-      const U k = kstage[s];
-      uint32_t d;
-      if constexpr (Digits::computed)
+      const uint32_t s = j * TPB + threadIdx.x;
+      if (full || s < valid)
       {
-        d = dg.stage[s];
-      }
-      else
-      {
-        d = extract_digit<U, FP>(k, bit, dmask);
-      }
-      const long long g = gdelta[d] + (long long) s;
-      if ((unsigned long long) g < out_limit)
-      {
-        __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
-        if constexpr (VB > 0)
+        const U k = kstage[s];
+        uint32_t d;
+        if constexpr (Digits::computed)
         {
-          __stcs(vout + g, vstage[s]);
+          d = dg.stage[s];
+        }
+        else
+        {
+          d = extract_digit<U, FP>(k, bit, dmask);
+        }
+        const long long g = gdelta[d] + (long long) s;
+        if ((unsigned long long) g < out_limit)
+        {
+          __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+          if constexpr (VB > 0)
+          {
+            __stcs(vout + g, vstage[s]);
+          }
         }
       }
     }

@@ -230,3 +230,25 @@ def test_unaligned_buffers_use_the_fallback_pass(oracle, offset):
     rk, rv = oracle.radix_sort(k[offset:], v[offset:])
     assert from_dev(ko, np.uint32).tobytes() == rk.tobytes()
     assert from_dev(vo, np.uint32).tobytes() == rv.tobytes()
+
+
+@pytest.mark.parametrize("case", ["top_digit_only", "low_digits_all_ones", "constant_then_random"])
+@pytest.mark.parametrize("dtype", [np.uint32, np.uint64, np.float32], ids=lambda d: np.dtype(d).name)
+def test_single_digit_tiles(oracle, dtype, case):
+    """Tiles whose keys all share the pass's digit take the direct-copy path; the digit may
+    equal the padding keys' digit of a partial tile (all ones)."""
+    n = 3_000_017
+    rng = np.random.default_rng(17)
+    u = I.UINT_OF[np.dtype(dtype).itemsize]
+    bits = np.dtype(dtype).itemsize * 8
+    if case == "top_digit_only":
+        k = (rng.integers(0, 256, n).astype(u) << u(bits - 8)) | u(0x5A)
+    elif case == "low_digits_all_ones":
+        low = (u(1) << u(bits - 8)) - u(1)
+        k = (rng.integers(0, 4, n).astype(u) << u(bits - 8)) | low
+    else:
+        k = I.uniform_bits(u, n, rng)
+        k[: n // 2] = u(0x1234)
+    k = k.view(dtype)
+    for desc in (False, True):
+        _check(oracle, k, I.index_values(n), desc=desc)
