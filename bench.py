@@ -4,9 +4,15 @@ Workload (one "step"): cub::DeviceRadixSort::SortPairs of 2^28 uint64 keys (unif
 the full 64-bit range, i.e. 64 bits of entropy) with uint32 values (value = original
 index), ascending, begin_bit 0 / end_bit 64, through the library's C ABI
 (cccl_device_radix_sort). Inputs (3.2 GB) exceed the 129 MB L2, so no flush is needed
-between steps. Variants of the same configuration (entropy 43.7/33.4/13.0-bit style
-AND-reduced keys, a constant key, descending, begin_bit 8 / end_bit 40) and the 2^28
-uint32 keys-only roofline row are reported under "variants".
+between steps. Reported beside the headline line:
+  * "variants": the same configuration at AND-reduced entropies, a constant key,
+    descending, begin_bit 8 / end_bit 40; 2^28 uint32 keys-only (the roofline row) and
+    2^24 uint32 keys-only with L2 flushed between steps;
+  * "segmented": the batched segmented sort of 2^27 f32 keys + i32 values in lognormal
+    segments, plain and CUDA-graph replay, against one plain sort launch per segment;
+  * "learned": the learned-partition sort against the plain sort on 2^28 f32 + u32
+    (Gaussian mixture, lognormal, Zipf) and 2^30 f64 + i64 DoubleBuffer inputs (lognormal,
+    lognormal/uniform mix, all-equal, sorted-then-reversed), bit-exactness checked.
 
 Metric: sorted keys per second (higher is better); roofline on HBM with algorithmic bytes
 = passes x N x 2 x (key + value bytes).
@@ -297,6 +303,127 @@ def run_segmented(torch, steps, per_segment_sample=4000):
     }
 
 
+def timed_median(torch, fn, reps, warmup=2, prep=None, flush=None):
+    """Median of per-step CUDA-event times (ms); prep (untimed) restores the input of an
+    in-place sort, flush (untimed) evicts L2 for inputs that fit in it."""
+    times = []
+    for i in range(warmup + reps):
+        if prep is not None:
+            prep()
+        if flush is not None:
+            flush()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        torch.cuda.synchronize()
+        if i >= warmup:
+            times.append(s.elapsed_time(e))
+    return statistics.median(times)
+
+
+def learned_keys(torch, dist, n, dtype, seed):
+    """Seeded synthetic keys of the learned-partition workloads, drawn on the GPU:
+    gmm (8 components, means U(-1e3, 1e3), sigmas log-uniform 1e-2..1e2), lognormal(0, 2)
+    for 4-byte and lognormal(0, 3) for 8-byte keys, zipf (s = 1.1 over 2^20 seeded uniform
+    values), mix (50/50 lognormal(0, 3) and U(0, 1)), all-equal, sorted-then-reversed."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    f64 = torch.float64
+    if dist == "gmm":
+        means = torch.rand(8, generator=g, device="cuda", dtype=f64) * 2e3 - 1e3
+        sig = 10 ** (torch.rand(8, generator=g, device="cuda", dtype=f64) * 4 - 2)
+        c = torch.randint(0, 8, (n,), generator=g, device="cuda")
+        x = means[c] + sig[c] * torch.randn(n, generator=g, device="cuda", dtype=f64)
+    elif dist == "lognormal":
+        x = torch.exp(torch.randn(n, generator=g, device="cuda", dtype=f64) * (2.0 if dtype == torch.float32 else 3.0))
+    elif dist == "zipf":
+        d = 1 << 20
+        w = torch.arange(1, d + 1, device="cuda", dtype=f64) ** -1.1
+        cdf = torch.cumsum(w, 0)
+        cdf /= cdf[-1].clone()
+        u = torch.rand(n, generator=g, device="cuda", dtype=f64)
+        r = torch.searchsorted(cdf, u, right=True).clamp_(max=d - 1)
+        x = (torch.rand(d, generator=g, device="cuda", dtype=f64) * 1e6)[r]
+    elif dist == "mix":
+        a = torch.exp(torch.randn(n, generator=g, device="cuda", dtype=f64) * 3.0)
+        b = torch.rand(n, generator=g, device="cuda", dtype=f64)
+        x = torch.where(torch.rand(n, generator=g, device="cuda") < 0.5, a, b)
+    elif dist == "all-equal":
+        x = torch.full((n,), 3.25, device="cuda", dtype=f64)
+    elif dist == "sorted-then-reversed":
+        x, _ = torch.sort(torch.exp(torch.randn(n, generator=g, device="cuda", dtype=f64) * 3.0))
+        x[n // 2 :] = torch.flip(x[n // 2 :], [0])
+    else:
+        raise ValueError(dist)
+    return x.to(dtype)
+
+
+def run_learned(torch, reps):
+    """Learned-partition sort vs the plain radix sort on the same GPU and inputs: the
+    Gaussian-mixture, lognormal and Zipf f32 workloads (2^28 keys + u32 values) and the
+    2^30 f64 + i64 DoubleBuffer workloads, adversarial inputs included. Every result is
+    checked bit for bit against the plain sort's."""
+    from cccl_gb300 import DoubleBuffer, SortOrder, make_learned_sort, make_radix_sort
+
+    peak, _ = _peaks()
+    cases = [("2^28 f32 + u32", d, 28, torch.float32, torch.int32, False) for d in ("gmm", "lognormal", "zipf")]
+    cases += [("2^30 f64 + i64, DoubleBuffer", d, 30, torch.float64, torch.int64, True)
+              for d in ("lognormal", "mix", "all-equal", "sorted-then-reversed")]
+    out = []
+    for label, dist, lg, kd, vd, overwrite in cases:
+        n = 1 << lg
+        k0 = learned_keys(torch, dist, n, kd, seed=11)
+        v0 = torch.arange(n, device="cuda", dtype=vd)
+        kb, vb = k0.element_size(), v0.element_size()
+        res = {"workload": f"{label}, {dist}", "num_items": n}
+        results = {}
+        for method, maker in (("plain", make_radix_sort), ("learned", make_learned_sort)):
+            k, v = (k0.clone(), v0.clone()) if overwrite else (k0, v0)
+            ko, vo = torch.empty_like(k0), torch.empty_like(v0)
+            if overwrite:
+                dk, dv = DoubleBuffer(k, ko), DoubleBuffer(v, vo)
+                args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
+
+                def prep():
+                    dk.d_buffers[dk.selector].copy_(k0)
+                    dv.d_buffers[dv.selector].copy_(v0)
+            else:
+                args = dict(d_in_keys=k, d_out_keys=ko, d_in_values=v, d_out_values=vo)
+                prep = None
+            s = maker(order=SortOrder.ASCENDING, **args)
+            tmp = torch.empty(s(temp_storage=None, num_items=n, **args), dtype=torch.uint8, device="cuda")
+            ms = timed_median(torch, lambda: s(temp_storage=tmp, num_items=n, **args), reps, prep=prep)
+            if prep is not None:
+                prep()
+            kt, _ = kernel_times_fn(torch, lambda: s(temp_storage=tmp, num_items=n, **args), steps=1)
+            res[method + "_ms"] = ms
+            res[method + "_keys_per_s"] = n / (ms / 1e3)
+            res[method + "_kernel_ms"] = {r: round(t, 4) for r, t in kt.items()}
+            if method == "learned":
+                res["learned_stats"] = s.stats(temp_storage=tmp, num_items=n, **args)
+            if overwrite:
+                results[method] = (dk.current().clone(), dv.current().clone(), dk.selector)
+            else:
+                results[method] = (ko.clone(), vo.clone(), None)
+            del tmp, s, k, v, ko, vo
+            torch.cuda.empty_cache()
+        pk, pv, psel = results["plain"]
+        lk, lv, lsel = results["learned"]
+        res["bitexact_vs_plain"] = bool(torch.equal(pk.view(torch.uint8), lk.view(torch.uint8))
+                                        and torch.equal(pv, lv) and psel == lsel)
+        res["speedup_vs_plain"] = res["plain_ms"] / res["learned_ms"]
+        plain_bytes = (8 * kb // 8) * n * 2 * (kb + vb)  # 8-bit passes x N x 2 x (K + V)
+        res["roofline_frac_plain_bytes"] = {
+            m: plain_bytes / (res[m + "_ms"] / 1e3) / 1e9 / peak for m in ("plain", "learned")}
+        st = res["learned_stats"]
+        learned_bytes = (st["partition_passes"] + 1) * n * 2 * (kb + vb)
+        res["roofline_frac_learned_bytes"] = learned_bytes / (res["learned_ms"] / 1e3) / 1e9 / peak
+        out.append(res)
+        del k0, v0, results, pk, pv, lk, lv
+        torch.cuda.empty_cache()
+    return out
+
+
 def kernel_times_fn(torch, fn, steps=3):
     from cccl_gb300 import _bindings as B
 
@@ -464,11 +591,13 @@ def run_engine(args):
     e2e_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
     torch.cuda.synchronize()
 
-    # the batched segmented configuration
+    # the batched segmented configuration and the learned-partition workloads
     segmented = None
+    learned = None
     if not args.no_variants:
         segmented = run_segmented(torch, max(3, args.steps // 2))
         torch.cuda.empty_cache()
+        learned = run_learned(torch, max(3, args.steps // 2))
 
     # variants of the configuration and the keys-only roofline row
     variants = []
@@ -481,22 +610,29 @@ def run_engine(args):
             ("descending", dict(descending=True)),
             ("bits 8..40", dict(begin_bit=8, end_bit=40)),
             ("u32 keys-only 2^28", dict(u32=True)),
+            ("u32 keys-only 2^24 (L2 flushed between steps)", dict(u32=True, log2n=24)),
         ]
         del main
         torch.cuda.empty_cache()
+        flush_buf = torch.empty(1 << 28, dtype=torch.uint8, device="cuda")  # 256 MB > L2
         for name, sp in specs:
+            nv = 1 << sp.get("log2n", N_LOG2)
             if sp.get("u32"):
-                kk = make_inputs(torch, n, "u32", seed=5)
+                kk = make_inputs(torch, nv, "u32", seed=5)
                 s = Sorter(torch, kk, with_values=False)
             else:
                 kk = make_inputs(torch, n, "u64", ands=sp.get("ands", 1), constant=sp.get("constant", False), seed=3)
                 s = Sorter(torch, kk, with_values=True, descending=sp.get("descending", False),
                            begin_bit=sp.get("begin_bit", 0), end_bit=sp.get("end_bit"))
-            vms = time_steps(torch, s.run, max(3, args.steps // 2), 2, barrier)
+            if nv < n:
+                vms = timed_median(torch, s.run, max(3, args.steps // 2), flush=lambda: flush_buf.fill_(1))
+            else:
+                vms = time_steps(torch, s.run, max(3, args.steps // 2), 2, barrier)
             kt, _ = kernel_times(torch, s, 3)
             variants.append({
                 "name": name,
-                "keys_per_s": n / (vms / 1000.0),
+                "num_items": nv,
+                "keys_per_s": nv / (vms / 1000.0),
                 "ms": vms,
                 "passes": s.passes,
                 "roofline_frac": s.algorithmic_bytes() / (vms / 1000.0) / 1e9 / peak,
@@ -505,6 +641,7 @@ def run_engine(args):
             })
             del s, kk
             torch.cuda.empty_cache()
+        del flush_buf
 
     if rank != 0:
         return
@@ -545,6 +682,7 @@ def run_engine(args):
         "cpu_baseline": cpu,
         "variants": variants,
         "segmented": segmented,
+        "learned": learned,
     }
     print(json.dumps(line))
 
