@@ -580,12 +580,28 @@ def run_engine(args):
     ok = torch.empty_like(hk, pin_memory=True)
     ov = torch.empty_like(hv, pin_memory=True)
 
+    # keys and values cross the host link on two streams at once (separate copy engines)
+    cur = torch.cuda.current_stream()
+    side = [torch.cuda.Stream(), torch.cuda.Stream()]
+
     def e2e_step():
-        main.ki.view(torch.int64).copy_(hk, non_blocking=True)
-        main.vi.copy_(hv, non_blocking=True)
+        for st in side:
+            st.wait_stream(cur)
+        with torch.cuda.stream(side[0]):
+            main.ki.view(torch.int64).copy_(hk, non_blocking=True)
+        with torch.cuda.stream(side[1]):
+            main.vi.copy_(hv, non_blocking=True)
+        for st in side:
+            cur.wait_stream(st)
         main.run()
-        ok.copy_(main.ko.view(torch.int64), non_blocking=True)
-        ov.copy_(main.vo, non_blocking=True)
+        for st in side:
+            st.wait_stream(cur)
+        with torch.cuda.stream(side[0]):
+            ok.copy_(main.ko.view(torch.int64), non_blocking=True)
+        with torch.cuda.stream(side[1]):
+            ov.copy_(main.vo, non_blocking=True)
+        for st in side:
+            cur.wait_stream(st)
 
     e2e_steps = max(3, args.steps // 2)
     e2e_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
@@ -699,8 +715,9 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile-case", choices=["pairs", "keys"],
-                    help="run two untimed sorts of 2^--log2n keys (u64+u32 pairs or u32 keys) for ncu captures")
+    ap.add_argument("--profile-case", choices=["pairs", "keys", "learned-f32", "learned-f64", "segmented"],
+                    help="run untimed sorts for ncu captures: 2^--log2n u64+u32 pairs or u32 keys (two sorts), "
+                         "one learned sort of 2^--log2n lognormal f32+i32 / f64+i64 pairs, or the segmented workload")
     ap.add_argument("--log2n", type=int, default=24)
     args = ap.parse_args()
     if args.profile_case:
@@ -708,12 +725,25 @@ def main():
 
         ensure_built()
         n = 1 << args.log2n
-        if args.profile_case == "pairs":
-            s = Sorter(torch, make_inputs(torch, n, "u64"), with_values=True)
+        if args.profile_case.startswith("learned"):
+            from cccl_gb300 import SortOrder, make_learned_sort
+
+            kd, vd = (torch.float32, torch.int32) if args.profile_case.endswith("f32") else (torch.float64, torch.int64)
+            k = learned_keys(torch, "lognormal", n, kd, seed=11)
+            v = torch.arange(n, device="cuda", dtype=vd)
+            la = dict(d_in_keys=k, d_out_keys=torch.empty_like(k), d_in_values=v, d_out_values=torch.empty_like(v))
+            ls = make_learned_sort(order=SortOrder.ASCENDING, **la)
+            tmp = torch.empty(ls(temp_storage=None, num_items=n, **la), dtype=torch.uint8, device="cuda")
+            ls(temp_storage=tmp, num_items=n, **la)
+        elif args.profile_case == "segmented":
+            run_segmented(torch, 1, per_segment_sample=10)
         else:
-            s = Sorter(torch, make_inputs(torch, n, "u32"), with_values=False)
-        s.run()
-        s.run()
+            if args.profile_case == "pairs":
+                s = Sorter(torch, make_inputs(torch, n, "u64"), with_values=True)
+            else:
+                s = Sorter(torch, make_inputs(torch, n, "u32"), with_values=False)
+            s.run()
+            s.run()
         torch.cuda.synchronize()
         print(f"profile case {args.profile_case} n=2^{args.log2n} done")
         return
