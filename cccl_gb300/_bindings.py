@@ -194,6 +194,7 @@ EXPORTED_SYMBOLS = [
     "cccl_gb300_learned_sort",
     "cccl_gb300_learned_sort_stats",
     "cccl_gb300_learned_sort_cleanup",
+    "cccl_gb300_segmented_radix_sort",
 ]
 
 NOALLOC_MAX_ITEMS = 1 << 20  # CCCL_GB300_NOALLOC_MAX_ITEMS
@@ -263,6 +264,8 @@ def _declare(lib):
     lib.cccl_gb300_set_launch_observer.restype = None
     lib.cccl_gb300_radix_sort_u32_noalloc.argtypes = [
         C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_bool, C.c_void_p]
+    lib.cccl_gb300_segmented_radix_sort.argtypes = list(lib.cccl_device_segmented_sort.argtypes[:11]) + [
+        C.c_int, C.c_int] + list(lib.cccl_device_segmented_sort.argtypes[11:])
     L = P(LearnedSortBuildResult)
     lib.cccl_gb300_learned_sort_build.argtypes = [L, C.c_int, Iterator, Iterator, C.c_int, C.c_int]
     lib.cccl_gb300_learned_sort.argtypes = [LearnedSortBuildResult] + list(lib.cccl_device_radix_sort.argtypes[1:])

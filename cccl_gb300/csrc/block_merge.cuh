@@ -50,7 +50,7 @@ struct BlockMergeSmem
   static constexpr size_t bytes    = ibuf_off + ((2 * islots + 15) / 16) * 16;
 };
 
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS>
 __device__ __forceinline__ void block_merge_sort_body(
   const void* keys_in, void* keys_out, const void* values_in, void* values_out, uint32_t num_items, const KeyCodec& codec)
 {

@@ -102,7 +102,7 @@ __device__ __forceinline__ int learned_leaf(U k, const LearnedTables<U>& t)
 // conversion of (key - knot) to float, the fused multiply-add with a slope >= 0, the clamp
 // to the leaf's rank range (leaf j's top equals leaf j+1's bottom) and the truncation after
 // scaling by a power of two.
-template <class U, bool FP>
+template <class U, int FP>
 __device__ __forceinline__ uint32_t
 learned_bucket(U enc, const LearnedTables<U>& t, float scale, uint32_t bmax)
 {
@@ -137,7 +137,7 @@ __device__ __forceinline__ uint32_t learned_mix(uint32_t x)
   return x;
 }
 
-template <int KB, bool FP>
+template <int KB, int FP>
 __device__ __forceinline__ void learned_sample_body(const LearnedSampleParams& p)
 {
   using U            = typename uint_of<KB>::type;
@@ -261,7 +261,7 @@ __device__ __forceinline__ void learned_cells_body(const LearnedFitParams& p)
 // ---------------------------------------------------------------------------------------
 // hist: digit counts of every partition pass in one read of the keys
 // ---------------------------------------------------------------------------------------
-template <int KB, bool FP, int TPB>
+template <int KB, int FP, int TPB>
 __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
 {
   using U         = typename uint_of<KB>::type;
@@ -297,7 +297,7 @@ __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
 // ---------------------------------------------------------------------------------------
 // pass: hook of the persistent onesweep pass that supplies the bucket id's digit
 // ---------------------------------------------------------------------------------------
-template <class U, bool FP>
+template <class U, int FP>
 struct LearnedPassHook
 {
   const LearnedModel* model;
@@ -331,7 +331,7 @@ struct LearnedPassHook
   }
 };
 
-template <int KB, int VB, bool FP>
+template <int KB, int VB, int FP>
 __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
 {
   using U             = typename uint_of<KB>::type;
@@ -345,7 +345,7 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
 // ---------------------------------------------------------------------------------------
 // bounds: thread b finds the first index whose key is in a bucket >= b
 // ---------------------------------------------------------------------------------------
-template <int KB, bool FP>
+template <int KB, int FP>
 __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p)
 {
   using U = typename uint_of<KB>::type;

@@ -162,7 +162,7 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
 
     auto radix = [&](int rvb, int rkind, RadixPolicy& pol, RadixKernels& ks) {
       pol                       = make_radix_policy(kb, rvb, rkind);
-      const RadixKernelNames nm = radix_kernel_names(kb, rvb, rkind);
+      const RadixKernelNames nm = radix_kernel_names(kb, rvb, rkind, rkind == KIND_FLOAT && sort_order == CCCL_DESCENDING);
       ks.init                   = get_kernel(r.radix_library, nm.init);
       ks.histogram              = get_kernel(r.radix_library, nm.histogram);
       ks.onesweep               = get_kernel(r.radix_library, nm.onesweep);
@@ -175,7 +175,7 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
 
     s->seg_pol = make_segmented_policy(kb, int(vb), kind);
     char names[SK_COUNT][64];
-    segmented_kernel_names(kb, int(vb), kind, names);
+    segmented_kernel_names(kb, int(vb), kind, sort_order == CCCL_DESCENDING, names);
     for (int i = 0; i < SK_COUNT; ++i)
     {
       s->seg_ks.k[i] = get_kernel(r.segmented_library, names[i]);

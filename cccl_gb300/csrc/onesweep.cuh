@@ -69,7 +69,7 @@ struct ComputedDigits
 // Per-tile steps 1-4. Preconditions: whist is zero, keys[] hold the tile's encoded keys
 // (padding keys of a partial tile are all-ones), misc[1] says whether stores are
 // disabled. load_values(vals) is called once after the ranking to fill the values.
-template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE, class LoadValues, class Digits = RadixDigits>
+template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE, class LoadValues, class Digits = RadixDigits>
 __device__ __forceinline__ void onesweep_tile(
   const OnesweepParams& p,
   const uint32_t tile,
@@ -382,7 +382,7 @@ __device__ __forceinline__ void load_tile_values_global(
 // ---------------------------------------------------------------------------------------
 // CTA-per-tile kernel (dynamic tile ids taken in launch order guarantee forward progress)
 // ---------------------------------------------------------------------------------------
-template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE>
+template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE>
 __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
 {
   using L          = OnesweepSmem<KB, VB, TPB, ITEMS>;
@@ -461,7 +461,7 @@ struct PlainPassHook
   {}
 };
 
-template <int KB, int VB, bool FP, int TPB, int ITEMS, bool STABLE, class Hook = PlainPassHook, size_t EXTRA = 0>
+template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE, class Hook = PlainPassHook, size_t EXTRA = 0>
 __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p, const Hook& hook = Hook{})
 {
   using L            = PersistentSmem<KB, VB, TPB, ITEMS, EXTRA>;

@@ -51,6 +51,16 @@
     gb300::histogram_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                                     \
   }
 
+// Single-tile kernels of descending floating-point sorts: CUB's single tile folds -0.0 into
+// +0.0 before ordering (see digit_source), unlike its onesweep passes.
+#define GB300_SINGLE_TILE_DESC_FP(KB)                   \
+  GB300_SINGLE_TILE(KB, 0, gb300::FP_BLOCK_DESC, fd)    \
+  GB300_SINGLE_TILE(KB, 1, gb300::FP_BLOCK_DESC, fd)    \
+  GB300_SINGLE_TILE(KB, 2, gb300::FP_BLOCK_DESC, fd)    \
+  GB300_SINGLE_TILE(KB, 4, gb300::FP_BLOCK_DESC, fd)    \
+  GB300_SINGLE_TILE(KB, 8, gb300::FP_BLOCK_DESC, fd)    \
+  GB300_SINGLE_TILE(KB, 16, gb300::FP_BLOCK_DESC, fd)
+
 #define GB300_ALL_VALUES(KB, FP, SUF)  \
   GB300_ONESWEEP(KB, 0, FP, SUF)       \
   GB300_ONESWEEP(KB, 1, FP, SUF)       \

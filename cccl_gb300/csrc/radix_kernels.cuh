@@ -161,7 +161,7 @@ __device__ __forceinline__ void histogram_for_each_key(const void* keys_v, unsig
 // histogram: counts of every pass's digit in one read; the last CTA writes the exclusive
 // prefix (global digit bases) of portion 0 for every pass. Also clears pass 0's look-back.
 // ---------------------------------------------------------------------------------------
-template <int KB, bool FP, int TPB>
+template <int KB, int FP, int TPB>
 __device__ __forceinline__ void histogram_body(const HistogramParams& p)
 {
   using U         = typename uint_of<KB>::type;
@@ -226,7 +226,7 @@ struct SingleTileSmem
 // Reads keys_in/values_in, writes keys_out/values_out (which may alias the inputs: all
 // reads complete before the first write). Starts with a CTA barrier so a persistent CTA
 // can call it for one segment after another.
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS>
 __device__ __forceinline__ void block_sort_body(
   const void* keys_in,
   void* keys_out,
@@ -396,7 +396,7 @@ __device__ __forceinline__ void block_sort_body(
   }
 }
 
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS>
 __device__ __forceinline__ void single_tile_body(const SingleTileParams& p)
 {
   block_sort_body<KB, VB, FP, TPB, ITEMS>(

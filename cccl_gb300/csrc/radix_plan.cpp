@@ -36,7 +36,7 @@ RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind)
   return p;
 }
 
-RadixKernelNames radix_kernel_names(int kb, int vb, int kind)
+RadixKernelNames radix_kernel_names(int kb, int vb, int kind, bool descending)
 {
   const std::string kv = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_" + (kind == KIND_FLOAT ? "f" : "i");
   RadixKernelNames n;
@@ -46,7 +46,8 @@ RadixKernelNames radix_kernel_names(int kb, int vb, int kind)
   n.onesweep_dyn = "gb300_onesweep_dyn_" + kv;
   // integer keys-only sorts have an order-free first-pass kernel
   n.onesweep_first = (vb == 0 && kind != KIND_FLOAT) ? "gb300_onesweep_first_" + kv : n.onesweep;
-  n.single_tile    = "gb300_single_tile_" + kv;
+  // descending float sorts: CUB's single tile folds -0.0 into +0.0 before ordering (FP_BLOCK_DESC)
+  n.single_tile = "gb300_single_tile_" + (kind == KIND_FLOAT && descending ? kv + "d" : kv);
   return n;
 }
 

@@ -51,7 +51,7 @@ struct RadixKernelNames
 {
   std::string init, histogram, onesweep, onesweep_first, onesweep_dyn, single_tile;
 };
-RadixKernelNames radix_kernel_names(int key_bytes, int value_bytes, int key_kind);
+RadixKernelNames radix_kernel_names(int key_bytes, int value_bytes, int key_kind, bool descending);
 
 struct RadixCall
 {

@@ -135,7 +135,7 @@ try
   *pol = make_radix_policy(key_bytes, int(value_size), kind);
   pol->magic = POLICY_MAGIC;
 
-  const RadixKernelNames names = radix_kernel_names(key_bytes, int(value_size), kind);
+  const RadixKernelNames names = radix_kernel_names(key_bytes, int(value_size), kind, sort_order == CCCL_DESCENDING);
   const std::string& one   = names.onesweep;
   const std::string& dyn   = names.onesweep_dyn;
   const std::string& first = names.onesweep_first;

@@ -505,7 +505,7 @@ __device__ __forceinline__ void seg_network_body(const SegSortParams& p, const u
 // ---------------------------------------------------------------------------------------
 // block class: one CTA per segment, shared-memory LSD passes
 // ---------------------------------------------------------------------------------------
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS>
 __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uint32_t* list, uint32_t count_index,
                                                uint32_t ticket_index)
 {
@@ -529,7 +529,8 @@ __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uin
     const uint32_t s  = list[item];
     const long long b = load_offset(p.begin_offsets, s, p.offsets_64);
     const uint32_t n  = uint32_t(load_offset(p.end_offsets, s, p.offsets_64) - b);
-    if constexpr (seg_block_algo(KB) == SEG_BLOCK_MERGE)
+    // the merge sort orders by the whole key; a bit window takes the radix block sort
+    if (seg_block_algo(KB) == SEG_BLOCK_MERGE && p.begin_bit == 0 && p.end_bit == 8 * KB)
     {
       block_merge_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
                                                     static_cast<U*>(p.keys_out) + b,
@@ -545,8 +546,8 @@ __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uin
                                               VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
                                               VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
                                               n,
-                                              0,
-                                              8 * KB,
+                                              p.begin_bit,
+                                              p.end_bit,
                                               p.codec);
     }
   }
@@ -557,7 +558,7 @@ __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uin
 // ---------------------------------------------------------------------------------------
 // Per-segment digit counts of every pass (one read of the large segments), and the
 // clearing of pass 0's look-back rows.
-template <int KB, bool FP, int TPB>
+template <int KB, int FP, int TPB>
 __device__ __forceinline__ void seg_device_histogram_body(const SegDeviceParams& p)
 {
   using U         = typename uint_of<KB>::type;
@@ -653,7 +654,7 @@ __device__ __forceinline__ void seg_device_scan_body(const SegDeviceParams& p)
 
 // One digit pass over all large segments: CTAs take tiles in ticket order (forward progress:
 // a tile only waits on lower tiles of its own segment, already taken by running CTAs).
-template <int KB, int VB, bool FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS>
 __device__ __forceinline__ void seg_device_onesweep_body(const SegDeviceParams& dp)
 {
   const int pass = dp.pass;

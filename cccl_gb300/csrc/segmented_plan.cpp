@@ -27,11 +27,14 @@ uint64_t ceil_div(uint64_t a, uint64_t b)
 }
 } // namespace
 
-void segmented_kernel_names(int kb, int vb, int kind, char (&names)[SK_COUNT][64])
+void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&names)[SK_COUNT][64])
 {
+  // descending float radix classes fold -0.0 into +0.0 before ordering, as CUB's block-radix
+  // paths do (FP_BLOCK_DESC); over whole keys the order is the same as the onesweep folding
+  const std::string fs  = kind == KIND_FLOAT ? (descending ? "fd" : "f") : "i";
   const std::string kv  = "k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_";
   const std::string net = kv + (kind == KIND_FLOAT ? "f" : kind == KIND_SIGNED ? "i" : "u");
-  const std::string rad = kv + (kind == KIND_FLOAT ? "f" : "i");
+  const std::string rad = kv + fs;
   const std::string n[SK_COUNT] = {
     "gb300_init",
     "gb300_seg_classify",
@@ -39,7 +42,7 @@ void segmented_kernel_names(int kb, int vb, int kind, char (&names)[SK_COUNT][64
     "gb300_seg_medium_" + net,
     "gb300_seg_block_s_" + rad,
     "gb300_seg_block_l_" + rad,
-    "gb300_seg_hist_k" + std::to_string(kb) + (kind == KIND_FLOAT ? "_f" : "_i"),
+    "gb300_seg_hist_k" + std::to_string(kb) + "_" + fs,
     "gb300_seg_scan",
     "gb300_seg_pass_" + rad};
   for (int i = 0; i < SK_COUNT; ++i)
@@ -83,27 +86,52 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   *selector           = 0;
 
   // ---- digit passes of the large segments and the buffer that receives the result ----
-  const int pass6_count = int(ceil_div(uint64_t(8 * kb), kb > 1 ? 6 : 4)); // CUB's radix passes
-  const int target      = c.target >= 0 ? c.target : c.overwrite ? (pass6_count & 1) : 1;
-  if (c.target >= 0 && !c.overwrite && c.target != 1)
+  // DeviceSegmentedSort: CUB's large segments take ceil(key bits / 6) passes (4-bit digits
+  // for 1-byte keys). DeviceSegmentedRadixSort (dispatch_segmented_radix_sort.cuh:734-745 and
+  // :519-526): max(ceil(window / R), 1) passes, R = 6 (5 for 1-byte keys), and the result is
+  // in the output buffer whenever overwriting is not allowed.
+  const int begin_bit = c.radix_only ? c.begin_bit : 0;
+  const int end_bit   = c.radix_only ? c.end_bit : 8 * kb;
+  if (begin_bit < 0 || end_bit > 8 * kb || begin_bit > end_bit)
   {
-    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "without overwrite the result goes to the output buffer");
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "begin_bit/end_bit outside the key");
   }
+  if (c.radix_only && begin_bit == end_bit && c.overwrite)
+  {
+    // nothing to sort and the caller takes the current buffer (dispatch_segmented_radix_sort.cuh:541)
+    if (c.d_temp_storage == nullptr)
+    {
+      *c.temp_storage_bytes = 1;
+    }
+    return;
+  }
+  const int cub_passes = c.radix_only
+                         ? std::max<int>(int(ceil_div(uint64_t(end_bit - begin_bit), kb > 1 ? 6 : 5)), 1)
+                         : int(ceil_div(uint64_t(8 * kb), kb > 1 ? 6 : 4));
+  const int target = c.target >= 0 ? c.target : c.overwrite ? (cub_passes & 1) : 1;
   int bit[SEG_MAX_PASSES];
   int bits[SEG_MAX_PASSES];
   int passes = 0;
-  for (int b = 0; b < 8 * kb; b += RADIX_BITS)
+  for (int b = begin_bit; b < end_bit; b += RADIX_BITS)
   {
     bit[passes]  = b;
-    bits[passes] = RADIX_BITS;
+    bits[passes] = std::min(RADIX_BITS, end_bit - b);
     ++passes;
+  }
+  if (passes == 0)
+  {
+    // an empty window still moves every large segment once (a 0-bit pass is a copy)
+    bit[0]  = begin_bit;
+    bits[0] = 0;
+    passes  = 1;
   }
   if (c.overwrite && (passes & 1) != target)
   {
-    // split the last digit into two 4-bit passes: the parity now matches CUB's
-    bits[passes - 1] = 4;
-    bit[passes]      = bit[passes - 1] + 4;
-    bits[passes]     = 4;
+    // split the last digit into two passes (one may have 0 bits): the parity now matches
+    const int w      = bits[passes - 1];
+    bits[passes - 1] = (w + 1) / 2;
+    bit[passes]      = bit[passes - 1] + (w + 1) / 2;
+    bits[passes]     = w / 2;
     ++passes;
   }
 
@@ -204,13 +232,13 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.begin_offsets   = c.begin_offsets;
     p.end_offsets     = c.end_offsets;
     p.offsets_64      = c.offsets_64;
-    p.partition       = nseg > uint64_t(SEG_PARTITION_THRESHOLD);
+    p.partition       = !c.radix_only && nseg > uint64_t(SEG_PARTITION_THRESHOLD);
     p.num_segments    = nseg;
     p.num_items       = n;
     p.max_device_segments = max_dev;
     p.max_tiles       = max_tiles;
     p.small_tile      = pol.small_threads * pol.small_items;
-    p.medium_tile     = pol.medium_threads * pol.medium_items;
+    p.medium_tile     = c.radix_only ? 0 : pol.medium_threads * pol.medium_items; // no merge networks
     p.block_small_cap = pol.block_s_cap;
     p.block_large_cap = pol.block_l_cap;
     p.device_tile     = uint32_t(pass_tile);
@@ -242,7 +270,9 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.block_s_list  = lists + 2 * list_stride;
     p.block_l_list  = lists + 3 * list_stride;
     p.codec         = codec;
-    if (nseg > uint64_t(SEG_PARTITION_THRESHOLD))
+    p.begin_bit     = begin_bit;
+    p.end_bit       = end_bit;
+    if (!c.radix_only && nseg > uint64_t(SEG_PARTITION_THRESHOLD))
     {
       launch("seg_small", ks.k[SK_SMALL], unsigned(sms * occupancy(ks.k[SK_SMALL], SEG_NETWORK_TPB, pol.network_small_smem)),
              SEG_NETWORK_TPB, pol.network_small_smem, c.stream, p);

@@ -59,7 +59,7 @@ struct SegmentedKernels
 };
 
 // Kernel names of one (key width, value width, key kind) in the segmented image.
-void segmented_kernel_names(int kb, int vb, int kind, char (&names)[SK_COUNT][64]);
+void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&names)[SK_COUNT][64]);
 
 struct SegmentedCall
 {
@@ -76,6 +76,11 @@ struct SegmentedCall
   size_t* temp_storage_bytes;
   CUstream stream;
   int target; // buffer index that receives the result; -1: the one CUB's dispatch picks
+  // DeviceSegmentedRadixSort semantics: every segment is radix-sorted (no merge networks)
+  // by bits [begin_bit, end_bit), and the buffer follows that dispatch's pass count
+  bool radix_only;
+  int begin_bit;
+  int end_bit;
 };
 
 // Runs (or sizes, when d_temp_storage is null) one segmented sort; writes the selector

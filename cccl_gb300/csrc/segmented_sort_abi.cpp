@@ -1,10 +1,12 @@
 // C ABI of the batched segmented sort: cccl_device_segmented_sort_{build,build_ex,compile,
-// load,link_ltoir,serialize,deserialize,cleanup} and the run entry cccl_device_segmented_sort.
+// load,link_ltoir,serialize,deserialize,cleanup}, the run entry cccl_device_segmented_sort and
+// cccl_gb300_segmented_radix_sort (DeviceSegmentedRadixSort semantics, same build).
 //
 // Reference interface: c/parallel/include/cccl/c/segmented_sort.h:27-139, implemented in
 // c/parallel/src/segmented_sort.cu (run :859-985: null selector rejected :875-881, keys and
 // values must be pointers, offsets through iterators :916-917).
 #include <cccl/c/segmented_sort.h>
+#include <cccl_gb300/segmented_radix_sort.h>
 
 #include <memory>
 
@@ -52,6 +54,97 @@ void free_result(cccl_device_segmented_sort_build_result_t* b)
   {
     delete[] *p;
     *p = nullptr;
+  }
+}
+
+// The run of both entry points; radix_only selects DeviceSegmentedRadixSort's semantics.
+CUresult segmented_run(const char* who,
+                       cccl_device_segmented_sort_build_result_t build,
+                       void* d_temp_storage,
+                       size_t* temp_storage_bytes,
+                       cccl_iterator_t d_keys_in,
+                       cccl_iterator_t d_keys_out,
+                       cccl_iterator_t d_values_in,
+                       cccl_iterator_t d_values_out,
+                       uint64_t num_items,
+                       uint64_t num_segments,
+                       cccl_iterator_t start_offset_in,
+                       cccl_iterator_t end_offset_in,
+                       bool radix_only,
+                       int begin_bit,
+                       int end_bit,
+                       bool is_overwrite_okay,
+                       int* selector,
+                       CUstream stream)
+{
+  if (selector == nullptr)
+  {
+    fflush(stderr);
+    printf("\nERROR in %s(): selector cannot be nullptr\n", who);
+    fflush(stdout);
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (d_keys_in.type != CCCL_POINTER || d_keys_out.type != CCCL_POINTER || d_values_in.type != CCCL_POINTER
+      || d_values_out.type != CCCL_POINTER)
+  {
+    fflush(stderr);
+    printf("\nERROR in %s(): keys and values must be pointers\n", who);
+    fflush(stdout);
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (start_offset_in.type != CCCL_POINTER || end_offset_in.type != CCCL_POINTER)
+  {
+    printf("\nERROR in %s(): segment offsets must be pointers\n", who);
+    return CUDA_ERROR_NOT_SUPPORTED;
+  }
+  const size_t osz = start_offset_in.value_type.size;
+  if ((osz != 4 && osz != 8) || end_offset_in.value_type.size != osz || temp_storage_bytes == nullptr)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  try
+  {
+    context_guard ctx;
+    if (build.runtime_policy == nullptr || build.runtime_policy_size != sizeof(SegmentedPolicy)
+        || static_cast<const SegmentedPolicy*>(build.runtime_policy)->magic != SEG_POLICY_MAGIC
+        || build.partition_runtime_policy == nullptr || build.library == nullptr)
+    {
+      return CUDA_ERROR_NOT_INITIALIZED;
+    }
+    const auto& pol = *static_cast<const SegmentedPolicy*>(build.runtime_policy);
+    const auto& tab = *static_cast<const SegKernelTable*>(build.partition_runtime_policy);
+    SegmentedKernels ks{};
+    for (int i = 0; i < SK_COUNT; ++i)
+    {
+      ks.k[i] = tab.handles[i];
+    }
+    SegmentedCall call{};
+    call.keys[0]            = d_keys_in.state;
+    call.keys[1]            = d_keys_out.state;
+    call.values[0]          = d_values_in.state;
+    call.values[1]          = d_values_out.state;
+    call.num_items          = num_items;
+    call.num_segments       = num_segments;
+    call.begin_offsets      = start_offset_in.state;
+    call.end_offsets        = end_offset_in.state;
+    call.offsets_64         = osz == 8 ? 1 : 0;
+    call.overwrite          = is_overwrite_okay;
+    call.descending         = build.order == CCCL_DESCENDING;
+    call.d_temp_storage     = d_temp_storage;
+    call.temp_storage_bytes = temp_storage_bytes;
+    call.stream             = stream;
+    call.target             = -1;
+    call.radix_only         = radix_only;
+    call.begin_bit          = begin_bit;
+    call.end_bit            = end_bit;
+    int sel                 = 0;
+    segmented_sort_dispatch(pol, ks, call, &sel);
+    *selector = sel;
+    return CUDA_SUCCESS;
+  }
+  catch (const std::exception& e)
+  {
+    return report(who, e);
   }
 }
 
@@ -113,7 +206,7 @@ try
   *pol       = make_segmented_policy(kb, int(vb), kind);
   pol->magic = SEG_POLICY_MAGIC;
   tab->magic = SEG_TABLE_MAGIC;
-  segmented_kernel_names(kb, int(vb), kind, tab->names);
+  segmented_kernel_names(kb, int(vb), kind, sort_order == CCCL_DESCENDING, tab->names);
 
   cccl_device_segmented_sort_build_result_t r{};
   r.cc                            = cc_major * 10 + cc_minor;
@@ -268,72 +361,32 @@ CCCL_C_API CUresult cccl_device_segmented_sort(
   int* selector,
   CUstream stream)
 {
-  if (selector == nullptr)
-  {
-    fflush(stderr);
-    printf("\nERROR in cccl_device_segmented_sort(): selector cannot be nullptr\n");
-    fflush(stdout);
-    return CUDA_ERROR_UNKNOWN;
-  }
-  if (d_keys_in.type != CCCL_POINTER || d_keys_out.type != CCCL_POINTER || d_values_in.type != CCCL_POINTER
-      || d_values_out.type != CCCL_POINTER)
-  {
-    fflush(stderr);
-    printf("\nERROR in cccl_device_segmented_sort(): keys and values must be pointers\n");
-    fflush(stdout);
-    return CUDA_ERROR_UNKNOWN;
-  }
-  if (start_offset_in.type != CCCL_POINTER || end_offset_in.type != CCCL_POINTER)
-  {
-    printf("\nERROR in cccl_device_segmented_sort(): segment offsets must be pointers\n");
-    return CUDA_ERROR_NOT_SUPPORTED;
-  }
-  const size_t osz = start_offset_in.value_type.size;
-  if ((osz != 4 && osz != 8) || end_offset_in.value_type.size != osz || temp_storage_bytes == nullptr)
-  {
-    return CUDA_ERROR_INVALID_VALUE;
-  }
-  try
-  {
-    context_guard ctx;
-    if (build.runtime_policy == nullptr || build.runtime_policy_size != sizeof(SegmentedPolicy)
-        || static_cast<const SegmentedPolicy*>(build.runtime_policy)->magic != SEG_POLICY_MAGIC
-        || build.partition_runtime_policy == nullptr || build.library == nullptr)
-    {
-      return CUDA_ERROR_NOT_INITIALIZED;
-    }
-    const auto& pol = *static_cast<const SegmentedPolicy*>(build.runtime_policy);
-    const auto& tab = *static_cast<const SegKernelTable*>(build.partition_runtime_policy);
-    SegmentedKernels ks{};
-    for (int i = 0; i < SK_COUNT; ++i)
-    {
-      ks.k[i] = tab.handles[i];
-    }
-    SegmentedCall call{};
-    call.keys[0]            = d_keys_in.state;
-    call.keys[1]            = d_keys_out.state;
-    call.values[0]          = d_values_in.state;
-    call.values[1]          = d_values_out.state;
-    call.num_items          = num_items;
-    call.num_segments       = num_segments;
-    call.begin_offsets      = start_offset_in.state;
-    call.end_offsets        = end_offset_in.state;
-    call.offsets_64         = osz == 8 ? 1 : 0;
-    call.overwrite          = is_overwrite_okay;
-    call.descending         = build.order == CCCL_DESCENDING;
-    call.d_temp_storage     = d_temp_storage;
-    call.temp_storage_bytes = temp_storage_bytes;
-    call.stream             = stream;
-    call.target             = -1;
-    int sel                 = 0;
-    segmented_sort_dispatch(pol, ks, call, &sel);
-    *selector = sel;
-    return CUDA_SUCCESS;
-  }
-  catch (const std::exception& e)
-  {
-    return report("cccl_device_segmented_sort", e);
-  }
+  return segmented_run("cccl_device_segmented_sort", build, d_temp_storage, temp_storage_bytes, d_keys_in, d_keys_out,
+                       d_values_in, d_values_out, num_items, num_segments, start_offset_in, end_offset_in, false, 0, 0,
+                       is_overwrite_okay, selector, stream);
+}
+
+CCCL_GB300_API CUresult cccl_gb300_segmented_radix_sort(
+  cccl_device_segmented_sort_build_result_t build,
+  void* d_temp_storage,
+  size_t* temp_storage_bytes,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_keys_out,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t d_values_out,
+  uint64_t num_items,
+  uint64_t num_segments,
+  cccl_iterator_t start_offset_in,
+  cccl_iterator_t end_offset_in,
+  int begin_bit,
+  int end_bit,
+  bool is_overwrite_okay,
+  int* selector,
+  CUstream stream)
+{
+  return segmented_run("cccl_gb300_segmented_radix_sort", build, d_temp_storage, temp_storage_bytes, d_keys_in,
+                       d_keys_out, d_values_in, d_values_out, num_items, num_segments, start_offset_in, end_offset_in,
+                       true, begin_bit, end_bit, is_overwrite_okay, selector, stream);
 }
 
 CCCL_C_API CUresult cccl_device_segmented_sort_link_ltoir(

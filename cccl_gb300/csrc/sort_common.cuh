@@ -77,20 +77,36 @@ __device__ __forceinline__ U decode_key(U t, const KeyCodec& c)
   return U(t ^ U((t & high_bit<U>()) ? c.inv_set : c.inv_clr));
 }
 
-// Digit source: for floating-point keys the encoded -0.0 (0x7f..f in both orders) is
-// replaced by the encoded +0.0 pattern (0x80..0) before the shift.
 // False when the kernel is gated off (see KernelGate).
 __device__ __forceinline__ bool gate_open(const KernelGate& g)
 {
   return g.gate == nullptr || (__ldcg(g.gate) & g.gate_mask) != 0u;
 }
 
-template <class U, bool FP>
+// Key modes (the FP template argument) and the digit source of an encoded key:
+//   FP_NONE: integer keys, the encoded key itself;
+//   FP_ONESWEEP: -0.0 and +0.0 both take the encoded pattern 0x80..0, in either order. CUB's
+//     onesweep complements descending keys after twiddling and then folds the twiddled -0.0
+//     pattern (cub/cub/block/radix_rank_sort_operations.cuh:43-80);
+//   FP_BLOCK_DESC: descending sorts of CUB's block-radix paths (single tile, segmented radix
+//     sort), which fold -0.0 into +0.0 before ordering: in the complemented key both zeros
+//     take +0.0's pattern 0x7f..f.
+// Over the whole key the two give one order (the patterns are adjacent); under a bit window
+// the zeros' window bits differ, and each path must match its CUB counterpart.
+constexpr int FP_NONE       = 0;
+constexpr int FP_ONESWEEP   = 1;
+constexpr int FP_BLOCK_DESC = 2;
+
+template <class U, int FP>
 __device__ __forceinline__ U digit_source(U t)
 {
-  if constexpr (FP)
+  if constexpr (FP == FP_ONESWEEP)
   {
     return (t == U(~high_bit<U>())) ? high_bit<U>() : t;
+  }
+  else if constexpr (FP == FP_BLOCK_DESC)
+  {
+    return (t == high_bit<U>()) ? U(~high_bit<U>()) : t;
   }
   else
   {
@@ -98,7 +114,7 @@ __device__ __forceinline__ U digit_source(U t)
   }
 }
 
-template <class U, bool FP>
+template <class U, int FP>
 __device__ __forceinline__ uint32_t extract_digit(U t, int bit, uint32_t mask)
 {
   return uint32_t(digit_source<U, FP>(t) >> bit) & mask;

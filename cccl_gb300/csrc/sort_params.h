@@ -184,6 +184,8 @@ struct SegSortParams
   const uint32_t* block_s_list;
   const uint32_t* block_l_list;
   KeyCodec codec;
+  int begin_bit; // key bits the block classes sort by
+  int end_bit;
 };
 
 struct SegDeviceParams

@@ -89,7 +89,7 @@ __device__ __forceinline__ uint32_t warp_match_digit(uint32_t d)
   return peers;
 }
 
-template <class U, bool FP, int ITEMS>
+template <class U, int FP, int ITEMS>
 __device__ __forceinline__ void warp_histogram(const U (&keys)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
 {
 #pragma unroll
@@ -125,7 +125,7 @@ __device__ __forceinline__ uint32_t block_digit_offsets(uint32_t* whist, uint32_
 }
 
 // Stable tile positions: pos[i] = whist_w[d] at the time key i is reached, in source order.
-template <class U, bool FP, int ITEMS>
+template <class U, int FP, int ITEMS>
 __device__ __forceinline__ void warp_rank_stable(
   const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
 {
@@ -186,7 +186,7 @@ warp_rank_stable_digits(const uint32_t (&dig)[ITEMS], uint32_t (&pos)[ITEMS], ui
 }
 
 // Order-free tile positions (same digit buckets, arbitrary order inside a bucket).
-template <class U, bool FP, int ITEMS>
+template <class U, int FP, int ITEMS>
 __device__ __forceinline__ void warp_rank_unstable(
   const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
 {

@@ -1,6 +1,7 @@
-// C++ entry points with the signatures of cub::DeviceRadixSort and cub::DeviceSegmentedSort,
-// running on this library's sm_103a kernels through its C ABI (cccl_device_radix_sort*,
-// cccl_device_segmented_sort*). Header-only; link the program with libccclsort.so.
+// C++ entry points with the signatures of cub::DeviceRadixSort, cub::DeviceSegmentedSort and
+// cub::DeviceSegmentedRadixSort, running on this library's sm_103a kernels through its C ABI
+// (cccl_device_radix_sort*, cccl_device_segmented_sort*, cccl_gb300_segmented_radix_sort).
+// Header-only; link the program with libccclsort.so.
 //
 // Mirrored signatures (reference files, cub/cub/device/):
 //   DeviceRadixSort (device_radix_sort.cuh): SortPairs :412 / DoubleBuffer :1127,
@@ -10,6 +11,9 @@
 //   DeviceSegmentedSort (device_segmented_sort.cuh): SortKeys :361, SortPairs :2468-2494 and
 //     the Descending, Stable and DoubleBuffer forms, with begin/end offsets given as
 //     pointers to 32- or 64-bit integers (iterators other than pointers are not taken).
+//   DeviceSegmentedRadixSort (device_segmented_radix_sort.cuh): SortPairs :234 / :417,
+//     SortPairsDescending :887 / :1073, SortKeys :1531 / :1702 and SortKeysDescending, with
+//     begin_bit / end_bit; values of 4 or 8 bytes.
 // Differences: the functions live in namespace cccl_gb300::cub (alias it to cub to switch
 // a program over); errors come back as cudaError_t (cudaErrorInvalidValue,
 // cudaErrorNotSupported, cudaErrorUnknown); decomposers and custom key types are not taken.
@@ -27,6 +31,7 @@
 
 #include <cccl/c/radix_sort.h>
 #include <cccl/c/segmented_sort.h>
+#include <cccl_gb300/segmented_radix_sort.h>
 
 #include <cstddef>
 #include <cstdint>
@@ -383,7 +388,8 @@ template <typename KeyT, typename ValueT, typename BeginT, typename EndT>
 cudaError_t segmented_sort(bool desc, void* d_temp_storage, size_t& temp_storage_bytes, const KeyT* keys_in,
                            KeyT* keys_out, const ValueT* values_in, ValueT* values_out, std::int64_t num_items,
                            std::int64_t num_segments, BeginT d_begin_offsets, EndT d_end_offsets, bool overwrite,
-                           int* selector, cudaStream_t stream)
+                           int* selector, cudaStream_t stream, bool radix_only = false, int begin_bit = 0,
+                           int end_bit = 0)
 {
   static_assert(std::is_pointer_v<BeginT> && std::is_pointer_v<EndT>, "segment offsets must be pointers");
   using BO = std::remove_cv_t<std::remove_pointer_t<BeginT>>;
@@ -421,21 +427,20 @@ cudaError_t segmented_sort(bool desc, void* d_temp_storage, size_t& temp_storage
     build = it->second.get();
   }
   int sel = 0;
-  const CUresult st = cccl_device_segmented_sort(
-    *build,
-    d_temp_storage,
-    &temp_storage_bytes,
-    pointer_it(keys_in, type_of<KeyT>::value, sizeof(KeyT)),
-    pointer_it(keys_out, type_of<KeyT>::value, sizeof(KeyT)),
-    vs ? pointer_it(values_in, vt, vs) : no_values(),
-    vs ? pointer_it(values_out, vt, vs) : no_values(),
-    std::uint64_t(num_items),
-    std::uint64_t(num_segments),
-    pointer_it(d_begin_offsets, offset_type<BO>(), sizeof(BO)),
-    pointer_it(d_end_offsets, offset_type<EO>(), sizeof(EO)),
-    overwrite,
-    &sel,
-    reinterpret_cast<CUstream>(stream));
+  const cccl_iterator_t ki = pointer_it(keys_in, type_of<KeyT>::value, sizeof(KeyT));
+  const cccl_iterator_t ko = pointer_it(keys_out, type_of<KeyT>::value, sizeof(KeyT));
+  const cccl_iterator_t vi = vs ? pointer_it(values_in, vt, vs) : no_values();
+  const cccl_iterator_t vo = vs ? pointer_it(values_out, vt, vs) : no_values();
+  const cccl_iterator_t bo = pointer_it(d_begin_offsets, offset_type<BO>(), sizeof(BO));
+  const cccl_iterator_t eo = pointer_it(d_end_offsets, offset_type<EO>(), sizeof(EO));
+  const CUresult st =
+    radix_only
+      ? cccl_gb300_segmented_radix_sort(*build, d_temp_storage, &temp_storage_bytes, ki, ko, vi, vo,
+                                        std::uint64_t(num_items), std::uint64_t(num_segments), bo, eo, begin_bit,
+                                        end_bit, overwrite, &sel, reinterpret_cast<CUstream>(stream))
+      : cccl_device_segmented_sort(*build, d_temp_storage, &temp_storage_bytes, ki, ko, vi, vo,
+                                   std::uint64_t(num_items), std::uint64_t(num_segments), bo, eo, overwrite, &sel,
+                                   reinterpret_cast<CUstream>(stream));
   if (selector != nullptr)
   {
     *selector = sel;
@@ -513,6 +518,124 @@ struct DeviceSegmentedSort
   CCCL_GB300_SEG_PAIRS(StableSortPairsDescending, true)
 #undef CCCL_GB300_SEG_KEYS
 #undef CCCL_GB300_SEG_PAIRS
+};
+
+// DeviceSegmentedRadixSort: radix order in every segment over bits [begin_bit, end_bit), the
+// returned DoubleBuffer selector follows that dispatch (dispatch_segmented_radix_sort.cuh:519-526).
+struct DeviceSegmentedRadixSort
+{
+  template <typename KeyT, typename ValueT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortPairs(void* d_temp_storage, size_t& temp_storage_bytes, const KeyT* d_keys_in, KeyT* d_keys_out,
+                               const ValueT* d_values_in, ValueT* d_values_out, std::int64_t num_items,
+                               std::int64_t num_segments, BeginOffsetIteratorT d_begin_offsets,
+                               EndOffsetIteratorT d_end_offsets, int begin_bit = 0, int end_bit = sizeof(KeyT) * 8,
+                               cudaStream_t stream = 0)
+  {
+    return detail::segmented_sort<KeyT, ValueT>(false, d_temp_storage, temp_storage_bytes, d_keys_in, d_keys_out,
+                                                d_values_in, d_values_out, num_items, num_segments, d_begin_offsets,
+                                                d_end_offsets, false, nullptr, stream, true, begin_bit, end_bit);
+  }
+  template <typename KeyT, typename ValueT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortPairsDescending(void* d_temp_storage, size_t& temp_storage_bytes, const KeyT* d_keys_in,
+                                         KeyT* d_keys_out, const ValueT* d_values_in, ValueT* d_values_out,
+                                         std::int64_t num_items, std::int64_t num_segments,
+                                         BeginOffsetIteratorT d_begin_offsets, EndOffsetIteratorT d_end_offsets,
+                                         int begin_bit = 0, int end_bit = sizeof(KeyT) * 8, cudaStream_t stream = 0)
+  {
+    return detail::segmented_sort<KeyT, ValueT>(true, d_temp_storage, temp_storage_bytes, d_keys_in, d_keys_out,
+                                                d_values_in, d_values_out, num_items, num_segments, d_begin_offsets,
+                                                d_end_offsets, false, nullptr, stream, true, begin_bit, end_bit);
+  }
+  template <typename KeyT, typename ValueT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortPairs(void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                               DoubleBuffer<ValueT>& d_values, std::int64_t num_items, std::int64_t num_segments,
+                               BeginOffsetIteratorT d_begin_offsets, EndOffsetIteratorT d_end_offsets,
+                               int begin_bit = 0, int end_bit = sizeof(KeyT) * 8, cudaStream_t stream = 0)
+  {
+    return db_pairs(false, d_temp_storage, temp_storage_bytes, d_keys, d_values, num_items, num_segments,
+                    d_begin_offsets, d_end_offsets, begin_bit, end_bit, stream);
+  }
+  template <typename KeyT, typename ValueT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortPairsDescending(void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                                         DoubleBuffer<ValueT>& d_values, std::int64_t num_items,
+                                         std::int64_t num_segments, BeginOffsetIteratorT d_begin_offsets,
+                                         EndOffsetIteratorT d_end_offsets, int begin_bit = 0,
+                                         int end_bit = sizeof(KeyT) * 8, cudaStream_t stream = 0)
+  {
+    return db_pairs(true, d_temp_storage, temp_storage_bytes, d_keys, d_values, num_items, num_segments,
+                    d_begin_offsets, d_end_offsets, begin_bit, end_bit, stream);
+  }
+  template <typename KeyT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortKeys(void* d_temp_storage, size_t& temp_storage_bytes, const KeyT* d_keys_in, KeyT* d_keys_out,
+                              std::int64_t num_items, std::int64_t num_segments, BeginOffsetIteratorT d_begin_offsets,
+                              EndOffsetIteratorT d_end_offsets, int begin_bit = 0, int end_bit = sizeof(KeyT) * 8,
+                              cudaStream_t stream = 0)
+  {
+    return detail::segmented_sort<KeyT, void>(false, d_temp_storage, temp_storage_bytes, d_keys_in, d_keys_out, nullptr,
+                                              nullptr, num_items, num_segments, d_begin_offsets, d_end_offsets, false,
+                                              nullptr, stream, true, begin_bit, end_bit);
+  }
+  template <typename KeyT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortKeysDescending(void* d_temp_storage, size_t& temp_storage_bytes, const KeyT* d_keys_in,
+                                        KeyT* d_keys_out, std::int64_t num_items, std::int64_t num_segments,
+                                        BeginOffsetIteratorT d_begin_offsets, EndOffsetIteratorT d_end_offsets,
+                                        int begin_bit = 0, int end_bit = sizeof(KeyT) * 8, cudaStream_t stream = 0)
+  {
+    return detail::segmented_sort<KeyT, void>(true, d_temp_storage, temp_storage_bytes, d_keys_in, d_keys_out, nullptr,
+                                              nullptr, num_items, num_segments, d_begin_offsets, d_end_offsets, false,
+                                              nullptr, stream, true, begin_bit, end_bit);
+  }
+  template <typename KeyT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortKeys(void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                              std::int64_t num_items, std::int64_t num_segments, BeginOffsetIteratorT d_begin_offsets,
+                              EndOffsetIteratorT d_end_offsets, int begin_bit = 0, int end_bit = sizeof(KeyT) * 8,
+                              cudaStream_t stream = 0)
+  {
+    return db_keys(false, d_temp_storage, temp_storage_bytes, d_keys, num_items, num_segments, d_begin_offsets,
+                   d_end_offsets, begin_bit, end_bit, stream);
+  }
+  template <typename KeyT, typename BeginOffsetIteratorT, typename EndOffsetIteratorT>
+  static cudaError_t SortKeysDescending(void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                                        std::int64_t num_items, std::int64_t num_segments,
+                                        BeginOffsetIteratorT d_begin_offsets, EndOffsetIteratorT d_end_offsets,
+                                        int begin_bit = 0, int end_bit = sizeof(KeyT) * 8, cudaStream_t stream = 0)
+  {
+    return db_keys(true, d_temp_storage, temp_storage_bytes, d_keys, num_items, num_segments, d_begin_offsets,
+                   d_end_offsets, begin_bit, end_bit, stream);
+  }
+
+private:
+  template <typename KeyT, typename ValueT, typename B, typename E>
+  static cudaError_t db_pairs(bool desc, void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                              DoubleBuffer<ValueT>& d_values, std::int64_t num_items, std::int64_t num_segments, B b,
+                              E e, int begin_bit, int end_bit, cudaStream_t stream)
+  {
+    int sel             = 0;
+    const cudaError_t r = detail::segmented_sort<KeyT, ValueT>(
+      desc, d_temp_storage, temp_storage_bytes, d_keys.Current(), d_keys.Alternate(), d_values.Current(),
+      d_values.Alternate(), num_items, num_segments, b, e, true, &sel, stream, true, begin_bit, end_bit);
+    if (r == cudaSuccess && d_temp_storage != nullptr)
+    {
+      d_keys.selector ^= sel;
+      d_values.selector = d_keys.selector;
+    }
+    return r;
+  }
+  template <typename KeyT, typename B, typename E>
+  static cudaError_t db_keys(bool desc, void* d_temp_storage, size_t& temp_storage_bytes, DoubleBuffer<KeyT>& d_keys,
+                             std::int64_t num_items, std::int64_t num_segments, B b, E e, int begin_bit, int end_bit,
+                             cudaStream_t stream)
+  {
+    int sel             = 0;
+    const cudaError_t r = detail::segmented_sort<KeyT, void>(
+      desc, d_temp_storage, temp_storage_bytes, d_keys.Current(), d_keys.Alternate(), nullptr, nullptr, num_items,
+      num_segments, b, e, true, &sel, stream, true, begin_bit, end_bit);
+    if (r == cudaSuccess && d_temp_storage != nullptr)
+    {
+      d_keys.selector ^= sel;
+    }
+    return r;
+  }
 };
 
 } // namespace cub

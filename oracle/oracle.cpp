@@ -101,14 +101,23 @@ uint64_t load_bits(const unsigned char* p, int bytes)
 
 } // namespace
 
-extern "C" uint64_t oracle_striped_key(uint64_t raw, int bytes, int kind, int begin_bit, int end_bit)
+// zero_to_minus: fold +0.0 into -0.0 instead of -0.0 into +0.0. That is the order CUB's
+// onesweep passes give a descending sort: they complement the twiddled keys and then fold the
+// twiddled -0.0 pattern (cub/cub/block/radix_rank_sort_operations.cuh:43-80), which in
+// uncomplemented terms leaves both zeros at -0.0's pattern. Only a bit window narrower than
+// the key can tell the two apart.
+extern "C" uint64_t oracle_striped_key_ex(uint64_t raw, int bytes, int kind, int begin_bit, int end_bit, int zero_to_minus)
 {
   const uint64_t all  = bytes == 8 ? ~0ull : ((1ull << (8 * bytes)) - 1ull);
   const uint64_t high = 1ull << (8 * bytes - 1);
   uint64_t key        = raw & all;
-  if (kind == 2 && key == high) // -0.0 becomes +0.0 before twiddling
+  if (kind == 2 && !zero_to_minus && key == high) // -0.0 becomes +0.0 before twiddling
   {
     key = 0;
+  }
+  if (kind == 2 && zero_to_minus && key == 0)
+  {
+    key = high;
   }
   if (kind == 1)
   {
@@ -127,6 +136,11 @@ extern "C" uint64_t oracle_striped_key(uint64_t raw, int bytes, int kind, int be
   return key;
 }
 
+extern "C" uint64_t oracle_striped_key(uint64_t raw, int bytes, int kind, int begin_bit, int end_bit)
+{
+  return oracle_striped_key_ex(raw, bytes, kind, begin_bit, end_bit, 0);
+}
+
 extern "C" {
 
 int oracle_radix_permutation(
@@ -141,7 +155,9 @@ int oracle_radix_permutation(
   std::vector<uint64_t> striped(n);
   for (uint64_t i = 0; i < n; ++i)
   {
-    striped[i] = oracle_striped_key(load_bits(kp + i * d.bytes, d.bytes), d.bytes, d.kind, begin_bit, end_bit);
+    // descending == 2: a descending sort with CUB onesweep's zero folding
+    striped[i] =
+      oracle_striped_key_ex(load_bits(kp + i * d.bytes, d.bytes), d.bytes, d.kind, begin_bit, end_bit, descending == 2);
   }
   std::iota(perm, perm + n, uint64_t(0));
   const uint64_t* s = striped.data();

@@ -8,6 +8,7 @@ extern "C" {
 
 /* Bit-ordered comparison key of one raw key (cub/test/catch2_radix_sort_helper.cuh:174-214). */
 uint64_t oracle_striped_key(uint64_t raw, int bytes, int kind, int begin_bit, int end_bit);
+uint64_t oracle_striped_key_ex(uint64_t raw, int bytes, int kind, int begin_bit, int end_bit, int zero_to_minus);
 
 /* Stable permutation that sorts `keys` (cccl_type_enum key_type) by their striped bits. */
 int oracle_radix_permutation(

@@ -58,8 +58,10 @@ def _ptr(a):
     return a.ctypes.data if a is not None and a.size else None
 
 
-def radix_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, threads=1):
-    """cub::DeviceRadixSort result for numpy ``keys`` (and ``values``)."""
+def radix_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, threads=1, onesweep_zeros=False):
+    """cub::DeviceRadixSort result for numpy ``keys`` (and ``values``). With
+    ``onesweep_zeros`` a descending sort folds +0.0 into -0.0, as CUB's onesweep passes do
+    (inputs larger than the single tile); it differs only under a bit window."""
     keys = np.ascontiguousarray(keys)
     if end_bit is None:
         end_bit = keys.dtype.itemsize * 8
@@ -72,7 +74,7 @@ def radix_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, t
         vb = values.dtype.itemsize
     rc = lib().oracle_radix_sort(
         TYPE_CODES[keys.dtype], _ptr(keys), _ptr(ko), vb, _ptr(values), _ptr(vo), keys.size,
-        begin_bit, end_bit, int(bool(descending)), threads,
+        begin_bit, end_bit, (2 if onesweep_zeros else 1) if descending else 0, threads,
     )
     if rc:
         raise ValueError(f"oracle_radix_sort rejected its arguments ({rc})")

@@ -2,6 +2,7 @@
 // library's cub-compatible shim (include/cccl_gb300/cub_shim.h) and compares every output
 // byte and every DoubleBuffer selector. Exit status 0 when all cases match.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_segmented_radix_sort.cuh>
 #include <cub/device/device_segmented_sort.cuh>
 
 #include <cccl_gb300/cub_shim.h>
@@ -270,6 +271,66 @@ void segmented_keys_db_case(const char* name, const std::vector<K>& hk)
   }
 }
 
+template <class K, class V, class O, bool DESC>
+void segmented_radix_pairs_case(const char* name, const std::vector<K>& hk, const std::vector<V>& hv, int b, int e)
+{
+  const size_t n = hk.size();
+  std::vector<O> hb, he;
+  random_segments(n, hb, he);
+  const size_t ns = hb.size();
+  O *db = to_dev(hb), *de = to_dev(he);
+  K *ki = to_dev(hk), *ko_c = to_dev(hk), *ko_s = to_dev(hk);
+  V *vi = to_dev(hv), *vo_c = to_dev(hv), *vo_s = to_dev(hv);
+  run([&](void* t, size_t& s) {
+    return DESC ? cub::DeviceSegmentedRadixSort::SortPairsDescending(t, s, ki, ko_c, vi, vo_c, n, ns, db, de, b, e)
+                : cub::DeviceSegmentedRadixSort::SortPairs(t, s, ki, ko_c, vi, vo_c, n, ns, db, de, b, e);
+  });
+  run([&](void* t, size_t& s) {
+    return DESC ? shim::DeviceSegmentedRadixSort::SortPairsDescending(t, s, ki, ko_s, vi, vo_s, n, ns, db, de, b, e)
+                : shim::DeviceSegmentedRadixSort::SortPairs(t, s, ki, ko_s, vi, vo_s, n, ns, db, de, b, e);
+  });
+  bool ok = same(name, "keys", from_dev(ko_c, n), from_dev(ko_s, n)) && same(name, "values", from_dev(vo_c, n), from_dev(vo_s, n));
+  std::printf("%s %s (%zu segments)\n", ok ? "PASS" : "FAIL", name, ns);
+  failures += !ok;
+  for (void* p : {(void*) db, (void*) de, (void*) ki, (void*) ko_c, (void*) ko_s, (void*) vi, (void*) vo_c, (void*) vo_s})
+  {
+    cudaFree(p);
+  }
+}
+
+template <class K, class O, bool DESC>
+void segmented_radix_keys_db_case(const char* name, const std::vector<K>& hk, int b, int e)
+{
+  const size_t n = hk.size();
+  std::vector<O> hb, he;
+  random_segments(n, hb, he);
+  const size_t ns = hb.size();
+  O *db = to_dev(hb), *de = to_dev(he);
+  K *a_c = to_dev(hk), *b_c = to_dev(hk), *a_s = to_dev(hk), *b_s = to_dev(hk);
+  cub::DoubleBuffer<K> dc(a_c, b_c);
+  shim::DoubleBuffer<K> ds(a_s, b_s);
+  run([&](void* t, size_t& s) {
+    return DESC ? cub::DeviceSegmentedRadixSort::SortKeysDescending(t, s, dc, n, ns, db, de, b, e)
+                : cub::DeviceSegmentedRadixSort::SortKeys(t, s, dc, n, ns, db, de, b, e);
+  });
+  run([&](void* t, size_t& s) {
+    return DESC ? shim::DeviceSegmentedRadixSort::SortKeysDescending(t, s, ds, n, ns, db, de, b, e)
+                : shim::DeviceSegmentedRadixSort::SortKeys(t, s, ds, n, ns, db, de, b, e);
+  });
+  bool ok = dc.selector == ds.selector;
+  if (!ok)
+  {
+    std::printf("FAIL %s: selector %d vs %d\n", name, dc.selector, ds.selector);
+  }
+  ok = ok && same(name, "keys", from_dev(dc.Current(), n), from_dev(ds.Current(), n));
+  std::printf("%s %s (%zu segments)\n", ok ? "PASS" : "FAIL", name, ns);
+  failures += !ok;
+  for (void* p : {(void*) db, (void*) de, (void*) a_c, (void*) b_c, (void*) a_s, (void*) b_s})
+  {
+    cudaFree(p);
+  }
+}
+
 int main()
 {
   {
@@ -295,6 +356,11 @@ int main()
   keys_db_case<double, true>("SortKeysDescending f64 DoubleBuffer", special_floats<double, unsigned long long>(777777), 0, 64);
   keys_db_case<double, false>("SortKeys f64 bits 3..50", special_floats<double, unsigned long long>(65537), 3, 50);
   keys_db_case<__half, false>("SortKeys f16 DoubleBuffer", random_bits<__half>(123457), 0, 16);
+  // descending float keys under a bit window: the single tile and the onesweep passes order the
+  // zeros differently in CUB itself
+  keys_db_case<float, true>("SortKeysDescending f32 bits 3..29 single tile", special_floats<float, unsigned>(4000), 3, 29);
+  keys_db_case<float, true>("SortKeysDescending f32 bits 3..29 onesweep", special_floats<float, unsigned>(300001), 3, 29);
+  keys_db_case<double, true>("SortKeysDescending f64 bits 0..50 single tile", special_floats<double, unsigned long long>(2000), 0, 50);
   {
     auto k = random_bits<unsigned>(4000);
     std::vector<unsigned char> v(k.size());
@@ -316,6 +382,22 @@ int main()
   }
   segmented_keys_db_case<unsigned long long, long long>("DeviceSegmentedSort SortKeysDescending u64 DoubleBuffer",
                                                         random_bits<unsigned long long>(1500001));
+  {
+    auto k = special_floats<float, unsigned>(2000003);
+    std::vector<int> v(k.size());
+    for (size_t i = 0; i < v.size(); ++i)
+    {
+      v[i] = int(i);
+    }
+    segmented_radix_pairs_case<float, int, int, false>("DeviceSegmentedRadixSort SortPairs f32+i32", k, v, 0, 32);
+    segmented_radix_pairs_case<float, int, int, true>("DeviceSegmentedRadixSort SortPairsDescending f32+i32 bits 3..29", k, v, 3, 29);
+  }
+  segmented_radix_keys_db_case<unsigned long long, long long, false>(
+    "DeviceSegmentedRadixSort SortKeys u64 DoubleBuffer bits 4..44", random_bits<unsigned long long>(1500001), 4, 44);
+  segmented_radix_keys_db_case<double, int, true>(
+    "DeviceSegmentedRadixSort SortKeysDescending f64 DoubleBuffer", special_floats<double, unsigned long long>(900001), 0, 64);
+  segmented_radix_keys_db_case<unsigned, int, false>(
+    "DeviceSegmentedRadixSort SortKeys u32 DoubleBuffer empty window", random_bits<unsigned>(300001), 7, 7);
   std::printf("%d failure(s)\n", failures);
   return failures == 0 ? 0 : 1;
 }

@@ -110,12 +110,13 @@ def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, ove
     return kres, vres, sel
 
 
-def gpu_seg_sort(keys, values, begin, end, descending=False, overwrite=False, offsets_dtype=np.int32):
-    """Sorts segments through cccl_device_segmented_sort. Output buffers start as copies of
-    the input so positions outside every segment compare equal. Returns (keys, values, selector)."""
+def gpu_seg_sort(keys, values, begin, end, descending=False, overwrite=False, offsets_dtype=np.int32, radix_bits=None):
+    """Sorts segments through cccl_device_segmented_sort, or with radix_bits=(begin_bit, end_bit)
+    through cccl_gb300_segmented_radix_sort. Output buffers start as copies of the input so
+    positions outside every segment compare equal. Returns (keys, values, selector)."""
     import torch
 
-    from cccl_gb300 import DoubleBuffer, SortOrder, make_segmented_sort
+    from cccl_gb300 import DoubleBuffer, SortOrder, make_segmented_radix_sort, make_segmented_sort
 
     order = SortOrder.DESCENDING if descending else SortOrder.ASCENDING
     ki = to_dev(keys)
@@ -132,8 +133,11 @@ def gpu_seg_sort(keys, values, begin, end, descending=False, overwrite=False, of
         args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
     else:
         args = dict(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo)
-    s = make_segmented_sort(order=order, start_offsets_in=bo, end_offsets_in=eo, **args)
+    maker = make_segmented_sort if radix_bits is None else make_segmented_radix_sort
+    s = maker(order=order, start_offsets_in=bo, end_offsets_in=eo, **args)
     call = dict(num_items=keys.size, num_segments=len(begin), start_offsets_in=bo, end_offsets_in=eo, **args)
+    if radix_bits is not None:
+        call.update(begin_bit=radix_bits[0], end_bit=radix_bits[1])
     nbytes = s(temp_storage=None, **call)
     temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
     s(temp_storage=temp, **call)

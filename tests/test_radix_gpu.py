@@ -252,3 +252,21 @@ def test_single_digit_tiles(oracle, dtype, case):
     k = k.view(dtype)
     for desc in (False, True):
         _check(oracle, k, I.index_values(n), desc=desc)
+
+
+@pytest.mark.parametrize("n", [2000, 300_001], ids=["single_tile", "onesweep"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64, np.float16], ids=lambda d: np.dtype(d).name)
+def test_descending_bit_window_zeros(oracle, dtype, n):
+    """Descending float sorts under a bit window: CUB's single tile folds -0.0 into +0.0,
+    its onesweep passes fold +0.0 into -0.0 (cub/cub/block/radix_rank_sort_operations.cuh:43-56),
+    and the two orders differ only here."""
+    from gpu_util import gpu_sort
+
+    rng = np.random.default_rng(n + np.dtype(dtype).itemsize)
+    k = I.with_specials(I.finite_floats(dtype, n, rng), rng, 1 / 8)
+    bits = np.dtype(dtype).itemsize * 8
+    for b, e in ((0, bits - 3), (3, bits - 5)):
+        ko, vo, _ = gpu_sort(k, I.index_values(n), b, e, True)
+        # 2000 pairs fit CUB's single tile for every key width here (>= 2304 with u32 values)
+        rk, rv = oracle.radix_sort(k, I.index_values(n), b, e, True, threads=4, onesweep_zeros=n > 2304)
+        assert ko.tobytes() == rk.tobytes() and vo.tobytes() == rv.tobytes()

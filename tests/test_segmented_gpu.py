@@ -118,3 +118,40 @@ def test_no_segments_and_no_items():
     k = np.arange(10, dtype=np.float32)
     ko, _, _ = gpu_seg_sort(k, None, np.array([], dtype=np.int64), np.array([], dtype=np.int64))
     assert ko.tobytes() == k.tobytes()
+
+
+# ---- DeviceSegmentedRadixSort semantics (cccl_gb300_segmented_radix_sort) ----
+def _radix_reference(oracle, keys, values, b, e, bits, desc):
+    """Per segment, the plain radix oracle over the bit window; positions outside every
+    segment keep the input."""
+    rk, rv = keys.copy(), (values.copy() if values is not None else None)
+    for lo, hi in zip(b, e):
+        if hi > lo:
+            sk, sv = oracle.radix_sort(keys[lo:hi], None if values is None else values[lo:hi], bits[0], bits[1], desc,
+                                       threads=1)
+            rk[lo:hi] = sk
+            if values is not None:
+                rv[lo:hi] = sv
+    return rk, rv
+
+
+@pytest.mark.parametrize("bits", [(0, None), (3, 29), (8, 8)], ids=["full", "window", "empty"])
+@pytest.mark.parametrize("desc", [False, True])
+@pytest.mark.parametrize("overwrite", [False, True], ids=["out", "doublebuffer"])
+def test_segmented_radix_sort(oracle, bits, desc, overwrite):
+    from gpu_util import gpu_seg_sort
+
+    rng = np.random.default_rng(31 + desc + 2 * overwrite)
+    b, e = edge_segments([1, 17, 112, 113, 2048, 2049, 8193, 30000, 5, 0, 700], gap=3)[:2]
+    n = int(e[-1]) + 5
+    k = I.with_specials(I.finite_floats(np.float32, n, rng), rng, 1 / 16)
+    v = I.index_values(n)
+    window = (bits[0], 32 if bits[1] is None else bits[1])
+    ko, vo, sel = gpu_seg_sort(k, v, b, e, desc, overwrite, radix_bits=window)
+    rk, rv = _radix_reference(oracle, k, v, b, e, window, desc)
+    assert ko.tobytes() == rk.tobytes() and vo.tobytes() == rv.tobytes()
+    if overwrite:
+        # DeviceSegmentedRadixSort: selector = max(ceil(bits / 6), 1) & 1; no bits and a
+        # DoubleBuffer: nothing runs (dispatch_segmented_radix_sort.cuh:541)
+        expect = 0 if window[0] == window[1] else max(-(-(window[1] - window[0]) // 6), 1) % 2
+        assert sel == expect
