@@ -57,10 +57,10 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
     gb300::seg_block_body<KB, VB, FP, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)>(                     \
       p, p.block_l_list, gb300::SEG_CTR_BLOCK_L, gb300::SEG_CTR_TICKET_BLOCK_L);                                     \
   }                                                                                                                  \
-  extern "C" __global__ void __launch_bounds__(gb300::SEG_PASS_TPB)                                                  \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_pass_tpb(KB, VB))                                         \
     gb300_seg_pass_k##KB##_v##VB##_##FS(const gb300::SegDeviceParams p)                                              \
   {                                                                                                                  \
-    gb300::seg_device_onesweep_body<KB, VB, FP, gb300::SEG_PASS_TPB, gb300::onesweep_items(KB, VB)>(p);              \
+    gb300::seg_device_onesweep_body<KB, VB, FP, gb300::seg_pass_tpb(KB, VB), gb300::seg_pass_items(KB, VB)>(p);      \
   }
 
 #define GB300_SEG_HIST(KB, FP, FS)                                                                                   \

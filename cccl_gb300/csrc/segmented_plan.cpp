@@ -63,15 +63,15 @@ SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
   p.medium_items        = seg_medium_items(kb, vb);
   p.block_s_cap         = SEG_BLOCK_S_CAP;
   p.block_l_cap         = SEG_BLOCK_L_CAP;
-  p.pass_tpb            = SEG_PASS_TPB;
-  p.pass_items          = onesweep_items(kb, vb);
+  p.pass_tpb            = seg_pass_tpb(kb, vb);
+  p.pass_items          = seg_pass_items(kb, vb);
   p.network_small_smem  = seg_network_smem(kb, vb, p.small_threads, p.small_items);
   p.network_medium_smem = seg_network_smem(kb, vb, p.medium_threads, p.medium_items);
   p.block_s_tpb         = seg_block_s_tpb(kb);
   p.block_l_tpb         = seg_block_l_tpb(kb);
   p.block_s_smem        = seg_block_smem(kb, seg_block_s_tpb(kb), seg_block_s_items(kb));
   p.block_l_smem        = seg_block_smem(kb, seg_block_l_tpb(kb), seg_block_l_items(kb));
-  p.pass_smem           = onesweep_smem_bytes(kb, vb);
+  p.pass_smem           = onesweep_smem_for(kb, vb, seg_pass_tpb(kb, vb), seg_pass_items(kb, vb));
   return p;
 }
 

@@ -64,6 +64,12 @@ GB300_HD constexpr size_t value_word_bytes(int vb)
 
 // Dynamic shared memory of the onesweep kernel: per-warp digit counters, per-digit
 // global deltas, a misc block, the key staging tile and (pairs) the value staging tile.
+GB300_HD constexpr size_t onesweep_smem_for(int kb, int vb, int tpb, int items)
+{
+  return size_t(4) * (tpb / 32) * 256 + size_t(8) * 256 + 128 + round16(size_t(kb) * tpb * items)
+       + (vb > 0 ? value_word_bytes(vb) * tpb * items : 0);
+}
+
 GB300_HD constexpr size_t onesweep_smem_bytes(int kb, int vb)
 {
   return size_t(4) * (ONESWEEP_TPB / 32) * 256 + size_t(8) * 256 + 128
@@ -220,7 +226,26 @@ GB300_HD constexpr int seg_block_l_tpb(int kb)
   return SEG_BLOCK_L_CAP / seg_block_l_items(kb);
 }
 constexpr int SEG_NETWORK_TPB   = 256;
-constexpr int SEG_PASS_TPB      = ONESWEEP_TPB;
+// Device-class digit pass (CTA per tile): threads and items per thread; GB300_SEG_PASS_*
+// override them in tuning builds. Measured on C3 (2^27 f32 + i32, seg_pass time): 384x16
+// 3.81 ms, 512x12 3.61, 768x8 3.57, 1024x8 3.17, 512x16 3.25, 256x16 5.34.
+// 8-byte keys or values keep 384 threads: at 1024 threads registers cap at 64 and spill.
+GB300_HD constexpr int seg_pass_tpb(int kb, int vb)
+{
+#ifdef GB300_SEG_PASS_TPB
+  return (void) kb, (void) vb, GB300_SEG_PASS_TPB;
+#else
+  return kb <= 4 && vb <= 4 ? 1024 : ONESWEEP_TPB;
+#endif
+}
+GB300_HD constexpr int seg_pass_items(int kb, int vb)
+{
+#ifdef GB300_SEG_PASS_ITEMS
+  return (void) kb, (void) vb, GB300_SEG_PASS_ITEMS;
+#else
+  return kb <= 4 && vb <= 4 ? 8 : onesweep_items(kb, vb);
+#endif
+}
 } // namespace gb300
 
 namespace gb300
