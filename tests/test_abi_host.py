@@ -166,3 +166,75 @@ def test_learned_run_rejects_what_the_plain_run_rejects(lib):
     op.name = b"decomposer"
     r = lib.cccl_gb300_learned_sort(b, None, C.byref(nbytes), it, it, it, it, op, 16, 0, 32, False, C.byref(sel), None)
     assert r == B.CUDA_ERROR_NOT_SUPPORTED
+
+
+# ---- segmented sort C ABI (c/parallel/include/cccl/c/segmented_sort.h), host side ----
+def _seg_compile(lib, key_type, value_type=None, order=0, cc=(10, 3), offset_type=None):
+    from cccl_gb300 import _bindings as B
+
+    offset_type = offset_type or (B.INT32, 4)
+    build = B.SegmentedSortBuildResult()
+    keys = B.pointer_iterator(0x1000, key_type[0], key_type[1])
+    vals = B.pointer_iterator(0x2000 if value_type else 0, *(value_type or (B.STORAGE, 4)))
+    offs = B.pointer_iterator(0x3000, offset_type[0], offset_type[1])
+    rc = lib.cccl_device_segmented_sort_compile(C.byref(build), order, keys, vals, offs, offs, cc[0], cc[1], None, None,
+                                                None, None, None)
+    return rc, build
+
+
+def test_segmented_compile_serialize_round_trip(lib):
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _seg_compile(lib, (B.FLOAT32, 4), (B.INT32, 4), order=B.DESCENDING)
+    assert rc == B.CUDA_SUCCESS and b.cc == 103 and b.payload and b.payload_size > 0
+    assert b.runtime_policy and b.partition_runtime_policy and b.order == B.DESCENDING
+    assert not b.library
+    buf, size = C.c_void_p(), C.c_size_t()
+    assert lib.cccl_device_segmented_sort_serialize(C.byref(b), C.byref(buf), C.byref(size)) == 0
+    b2 = B.SegmentedSortBuildResult()
+    assert lib.cccl_device_segmented_sort_deserialize(C.byref(b2), buf, size) == 0
+    assert b2.payload_size == b.payload_size and b2.order == b.order and b2.key_type.type == B.FLOAT32
+    assert C.string_at(b2.payload, b2.payload_size) == C.string_at(b.payload, b.payload_size)
+    assert C.string_at(b2.partition_runtime_policy, b2.partition_runtime_policy_size) == C.string_at(
+        b.partition_runtime_policy, b.partition_runtime_policy_size)
+    b3 = B.SegmentedSortBuildResult()
+    assert lib.cccl_device_segmented_sort_deserialize(C.byref(b3), buf, 12) != 0
+    lib.cccl_serialization_buffer_free(buf)
+    for x in (b, b2):
+        assert lib.cccl_device_segmented_sort_cleanup(C.byref(x)) == 0
+
+
+def test_segmented_compile_rejections(lib):
+    from cccl_gb300 import _bindings as B
+
+    assert _seg_compile(lib, (B.FLOAT32, 4), cc=(9, 0))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _seg_compile(lib, (B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _seg_compile(lib, (B.FLOAT32, 4), (B.STORAGE, 16))[0] == B.CUDA_ERROR_NOT_SUPPORTED
+    assert _seg_compile(lib, (B.FLOAT32, 4), order=5)[0] == B.CUDA_ERROR_INVALID_VALUE
+    assert lib.cccl_device_segmented_sort_cleanup(None) == B.CUDA_ERROR_INVALID_VALUE
+
+
+@pytest.mark.parametrize("entry", ["cccl_device_segmented_sort", "cccl_gb300_segmented_radix_sort"])
+def test_segmented_run_rejections(lib, entry):
+    """Checks made before any device work (segmented_sort.cu:875-917 for the reference entry)."""
+    from cccl_gb300 import _bindings as B
+
+    rc, b = _seg_compile(lib, (B.FLOAT32, 4), (B.INT32, 4))
+    assert rc == 0
+    fn = getattr(lib, entry)
+    it = B.pointer_iterator(0x1000, B.FLOAT32, 4)
+    off = B.pointer_iterator(0x3000, B.INT32, 4)
+    bad = B.pointer_iterator(0x1000, B.FLOAT32, 4)
+    bad.type = B.ITERATOR
+    narrow = B.pointer_iterator(0x3000, B.INT16, 2)
+    bits = (0, 32) if entry.endswith("radix_sort") else ()
+    nbytes, sel = C.c_size_t(0), C.c_int(-1)
+
+    def call(k=it, o=off, e=off, selector=C.byref(sel)):
+        return fn(b, None, C.byref(nbytes), k, it, it, it, 16, 2, o, e, *bits, False, selector, None)
+
+    assert call(selector=None) == B.CUDA_ERROR_UNKNOWN  # null selector
+    assert call(k=bad) == B.CUDA_ERROR_UNKNOWN  # keys must be pointers
+    assert call(o=bad) == B.CUDA_ERROR_NOT_SUPPORTED  # offsets through iterators
+    assert call(o=narrow, e=narrow) == B.CUDA_ERROR_INVALID_VALUE  # 16-bit offsets
+    lib.cccl_device_segmented_sort_cleanup(C.byref(b))
