@@ -60,6 +60,11 @@ SegmentedCall bucket_sort_call(const LearnedSetup& s, const RadixCall& c, const 
   sc.descending    = c.descending;
   sc.stream        = c.stream;
   sc.target        = 0;
+  // radix order in every bucket: the merge networks of small segments compare floats as
+  // floats (NaN placement), the plain sort orders bit patterns
+  sc.radix_only    = true;
+  sc.begin_bit     = 0;
+  sc.end_bit       = 8 * s.key_bytes;
   return sc;
 }
 } // namespace

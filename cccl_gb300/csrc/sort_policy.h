@@ -227,15 +227,16 @@ GB300_HD constexpr int seg_block_l_tpb(int kb)
 }
 constexpr int SEG_NETWORK_TPB   = 256;
 // Device-class digit pass (CTA per tile): threads and items per thread; GB300_SEG_PASS_*
-// override them in tuning builds. Measured on C3 (2^27 f32 + i32, seg_pass time): 384x16
-// 3.81 ms, 512x12 3.61, 768x8 3.57, 1024x8 3.17, 512x16 3.25, 256x16 5.34.
-// 8-byte keys or values keep 384 threads: at 1024 threads registers cap at 64 and spill.
+// override them in tuning builds. Measured (cccl_gb300/autotune.py, cccl_gb300/tuning_gb300.json,
+// lognormal segments of 2^26 keys, seg_pass time per sort): f32+i32 384x16 1.56 (shipped
+// before) / 384x12 2.19 / 512x12 1.73 / 1024x8 1.57 ms; f64+i64 384x12 4.93 / 512x12 4.24 /
+// 1024x8 4.13 ms (with a few spilled registers, still the fastest).
 GB300_HD constexpr int seg_pass_tpb(int kb, int vb)
 {
 #ifdef GB300_SEG_PASS_TPB
   return (void) kb, (void) vb, GB300_SEG_PASS_TPB;
 #else
-  return kb <= 4 && vb <= 4 ? 1024 : ONESWEEP_TPB;
+  return (void) kb, (void) vb, 1024;
 #endif
 }
 GB300_HD constexpr int seg_pass_items(int kb, int vb)
@@ -243,7 +244,7 @@ GB300_HD constexpr int seg_pass_items(int kb, int vb)
 #ifdef GB300_SEG_PASS_ITEMS
   return (void) kb, (void) vb, GB300_SEG_PASS_ITEMS;
 #else
-  return kb <= 4 && vb <= 4 ? 8 : onesweep_items(kb, vb);
+  return (void) kb, (void) vb, 8;
 #endif
 }
 } // namespace gb300

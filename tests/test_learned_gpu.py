@@ -140,3 +140,18 @@ def test_larger_bucket_count(oracle):
     k = I.lognormal(np.float32, n, rng, 0.0, 2.0)
     st = _check(oracle, k, I.index_values(n))
     assert st["bucket_log2"] == 13 and st["partition_passes"] == 2
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=lambda d: np.dtype(d).name)
+def test_sparse_buckets_with_specials(oracle, dtype):
+    """A dense cluster and a sparse tail: the tail's buckets hold a handful of keys, NaNs of
+    both signs and payloads, infinities and zeros among them; they must come out in radix
+    order (bit patterns), as the plain sort gives them."""
+    rng = np.random.default_rng(41)
+    n = N
+    k = rng.random(n).astype(dtype)
+    tail = rng.choice(n, size=n // 500, replace=False)
+    k[tail] = (10.0 ** rng.uniform(-30, 30, size=tail.size) * rng.choice([-1, 1], size=tail.size)).astype(dtype)
+    k = I.with_specials(k, rng, 1e-4)
+    for desc in (False, True):
+        _check(oracle, k, I.index_values(n), desc=desc)
