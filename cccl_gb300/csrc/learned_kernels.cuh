@@ -7,7 +7,7 @@
 //   hist    : one read of the keys: bucket of every key, digit counts of every partition pass;
 //   pass    : the persistent onesweep pass with the bucket id's digits in place of key bits
 //             (stable, so after the passes the keys are grouped by bucket in input order);
-//   bounds  : first index of every bucket, by binary search on the partitioned keys.
+//   bounds  : first index of every bucket, from one read of the partitioned keys.
 // The buckets are then sorted as segments by the batched segmented sort; a bucket too large
 // for a block sort goes to its plain radix passes.
 //
@@ -343,8 +343,14 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
-// bounds: thread b finds the first index whose key is in a bucket >= b
+// bounds: one read of the partitioned keys (bucket ids never decrease along them); where the
+// bucket id changes from a to b at index i, begins[b] = ends[a] = i, and the last key's bucket
+// ends at n. Empty buckets keep the zeros they were cleared to (begin == end). Warp w covers keys
+// [w * 32 * ITEMS, (w + 1) * 32 * ITEMS), lane l the keys l, l + 32, ...; the bucket of the
+// key before each comes from the neighbouring lane.
 // ---------------------------------------------------------------------------------------
+constexpr int LEARNED_BOUNDS_ITEMS = 16;
+
 template <int KB, int FP>
 __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p)
 {
@@ -353,36 +359,48 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
   learned_load_tables<U>(p.model, &tables);
   __syncthreads();
 
-  const unsigned long long nb = 1ull << p.bucket_log2;
-  const unsigned long long b  = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x;
-  if (b > nb)
+  const unsigned long long n   = p.num_items;
+  const float scale            = learned_scale(p.bucket_log2);
+  const uint32_t bmax          = (1u << p.bucket_log2) - 1;
+  const U* keys                = static_cast<const U*>(p.keys);
+  const int lane               = threadIdx.x & 31;
+  const unsigned long long warps_total = (unsigned long long) gridDim.x * (blockDim.x >> 5);
+  const unsigned long long chunk       = 32ull * LEARNED_BOUNDS_ITEMS;
+  auto bucket_at = [&](unsigned long long i) {
+    return learned_bucket<U, FP>(encode_key<U>(keys[i], p.codec), tables, scale, bmax);
+  };
+  for (unsigned long long w = blockIdx.x * (unsigned long long) (blockDim.x >> 5) + (threadIdx.x >> 5);
+       w * chunk < n; w += warps_total)
   {
-    return;
-  }
-  const unsigned long long n = p.num_items;
-  if (b == 0 || b == nb)
-  {
-    p.bounds[b] = b == 0 ? 0ull : n;
-    return;
-  }
-  const float scale   = learned_scale(p.bucket_log2);
-  const uint32_t bmax = uint32_t(nb - 1);
-  const U* keys       = static_cast<const U*>(p.keys);
-  unsigned long long lo = 0, hi = n;
-  while (lo < hi)
-  {
-    const unsigned long long mid = (lo + hi) >> 1;
-    const uint32_t bk = learned_bucket<U, FP>(encode_key<U>(keys[mid], p.codec), tables, scale, bmax);
-    if (bk < uint32_t(b))
+    const unsigned long long first = w * chunk;
+    // bucket of the key before this warp's chunk (none before index 0)
+    long long carry = first == 0 ? -1ll : (long long) bucket_at(first - 1);
+#pragma unroll 1
+    for (int it = 0; it < LEARNED_BOUNDS_ITEMS; ++it)
     {
-      lo = mid + 1;
-    }
-    else
-    {
-      hi = mid;
+      const unsigned long long i = first + (unsigned long long) it * 32 + lane;
+      const bool valid           = i < n;
+      const long long b          = valid ? (long long) bucket_at(i) : -2ll;
+      long long prev             = __shfl_up_sync(0xffffffffu, b, 1);
+      if (lane == 0)
+      {
+        prev = carry;
+      }
+      carry = __shfl_sync(0xffffffffu, b, 31);
+      if (valid && b != prev)
+      {
+        p.begins[b] = i; // a bucket starts here
+        if (prev >= 0)
+        {
+          p.ends[prev] = i; // and the one before it ends
+        }
+      }
+      if (i == n - 1)
+      {
+        p.ends[b] = n;
+      }
     }
   }
-  p.bounds[b] = lo;
 }
 
 } // namespace gb300

@@ -4,8 +4,9 @@
 // the same result and the same DoubleBuffer selector as the plain sort
 // (cub/cub/device/dispatch/dispatch_radix_sort.cuh:1698-1948 leaves the result of a
 // full-width sort of k-byte keys after k 8-bit passes, i.e. in the current buffer when k is
-// even). Bucket count: about 2^LEARNED_BUCKET_ITEMS_LOG2 keys per bucket, so that nearly
-// every bucket fits a block sort; the partition needs ceil(log2(buckets) / 8) stable passes.
+// even). Bucket count: about 2^LEARNED_BUCKET_ITEMS_LOG2 keys per bucket (the block sort
+// classes of the segmented sort); the partition needs
+// ceil(log2(buckets) / 8) stable passes.
 #include "learned_plan.h"
 
 #include <algorithm>
@@ -108,7 +109,7 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
   t.sample_temp_bytes = plan_radix_temp(s.sample_pol, LEARNED_SAMPLE, 0, 8 * kb, false, true).total_bytes;
   off += align_up(t.sample_temp_bytes, 256);
   t.bounds_off = off;
-  off += align_up(8 * ((size_t(1) << t.bucket_log2) + 1), 256);
+  off += align_up(2 * 8 * (size_t(1) << t.bucket_log2), 256); // begins, ends
   t.keys_tmp_off = off;
   if (!c.overwrite)
   {
@@ -184,7 +185,9 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
                          reinterpret_cast<uint32_t*>(base + t.lookback_off) + t.lookback_words};
   auto* model         = reinterpret_cast<LearnedModel*>(base + t.model_off);
   void* sample[2]     = {base + t.sample_off, base + t.sample_off + align_up(size_t(LEARNED_SAMPLE) * kb, 256)};
-  auto* bounds        = reinterpret_cast<unsigned long long*>(base + t.bounds_off);
+  auto* begins        = reinterpret_cast<unsigned long long*>(base + t.bounds_off);
+  auto* ends          = begins + (size_t(1) << t.bucket_log2);
+
   void* keys_tmp      = base + t.keys_tmp_off;
   void* values_tmp    = base + t.values_tmp_off;
   const KeyCodec codec = make_codec(s.key_kind, kb, c.descending);
@@ -316,18 +319,24 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
   }
   void* part_keys = kdst[P - 1];
   void* part_vals = has_vals ? vdst[P - 1] : nullptr;
-  // 7. first index of every bucket
+  // 7. begin and end of every bucket, from one read of the partitioned keys
   {
+    InitParams z{};
+    z.words     = reinterpret_cast<uint32_t*>(begins);
+    z.num_words = 4 * (uint64_t(1) << t.bucket_log2);
+    launch("learned_init", s.lk.init, unsigned(std::min<uint64_t>(ceil_div(z.num_words, 256), uint64_t(sms) * 8)),
+           256, 0, c.stream, z);
     LearnedBoundsParams p{};
     p.keys        = part_keys;
     p.num_items   = n;
     p.model       = model;
-    p.bounds      = bounds;
+    p.begins      = begins;
+    p.ends        = ends;
     p.codec       = codec;
     p.bucket_log2 = t.bucket_log2;
-    const uint64_t threads = (1ull << t.bucket_log2) + 1;
-    launch("learned_bounds", s.lk.bounds, unsigned(ceil_div(threads, LEARNED_BOUNDS_TPB)), LEARNED_BOUNDS_TPB, 0,
-           c.stream, p);
+    const uint64_t warps = ceil_div(n, 32ull * 16);
+    const unsigned grid  = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(warps, 8), uint64_t(sms) * 16)));
+    launch("learned_bounds", s.lk.bounds, grid, 256, 0, c.stream, p);
   }
   // 8. every bucket sorted as a segment; the result lands where the plain sort puts it
   {
@@ -343,8 +352,8 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     sc.keys[1]            = other_keys;
     sc.values[0]          = part_vals;
     sc.values[1]          = other_vals;
-    sc.begin_offsets      = bounds;
-    sc.end_offsets        = bounds + 1;
+    sc.begin_offsets      = begins;
+    sc.end_offsets        = ends;
     sc.target             = final_keys == part_keys ? 0 : 1;
     sc.d_temp_storage     = base + t.seg_off;
     size_t bytes          = t.seg_bytes;

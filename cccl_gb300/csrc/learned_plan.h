@@ -1,6 +1,6 @@
 // Host dispatcher of the learned-partition sort: sample -> plain radix sort of the sample
-// -> least-squares fit -> bucket histogram -> stable partition passes on the bucket id ->
-// bucket bounds -> batched segmented sort of the buckets. Inputs it does not take (fewer
+// -> least-squares fit -> digit counts -> stable partition passes on the bucket id -> bucket
+// bounds (one read of the partitioned keys) -> batched segmented sort of the buckets. Inputs it does not take (fewer
 // than LEARNED_MIN_ITEMS keys, a partial bit window, buffers that are not 16-byte aligned)
 // run the plain radix sort instead; the output and the selector are the plain sort's either way.
 #pragma once

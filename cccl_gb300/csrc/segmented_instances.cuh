@@ -70,5 +70,21 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
     gb300::seg_device_histogram_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                               \
   }
 
+// radix-order networks: KIND = NET_RADIX + FP mode, their own shapes
+#define GB300_SEG_RNETWORK(KB, KIND, KS, VB)                                                                         \
+  extern "C" __global__ void __launch_bounds__(gb300::SEG_NETWORK_TPB)                                               \
+    gb300_seg_small_k##KB##_v##VB##_##KS(const gb300::SegSortParams p)                                               \
+  {                                                                                                                  \
+    gb300::seg_network_body<KB, KIND, VB, gb300::SEG_RSMALL_THREADS, gb300::SEG_RSMALL_ITEMS>(                        \
+      p, p.small_list, gb300::SEG_CTR_SMALL, gb300::SEG_CTR_TICKET_SMALL);                                           \
+  }                                                                                                                  \
+  extern "C" __global__ void __launch_bounds__(gb300::SEG_NETWORK_TPB)                                               \
+    gb300_seg_medium_k##KB##_v##VB##_##KS(const gb300::SegSortParams p)                                              \
+  {                                                                                                                  \
+    gb300::seg_network_body<KB, KIND, VB, gb300::SEG_RMEDIUM_THREADS, gb300::SEG_RMEDIUM_ITEMS>(                      \
+      p, p.medium_list, gb300::SEG_CTR_MEDIUM, gb300::SEG_CTR_TICKET_MEDIUM);                                        \
+  }
+#define GB300_SEG_RNET_VALUES(KB, KIND, KS) GB300_SEG_RNETWORK(KB, KIND, KS, 0) GB300_SEG_RNETWORK(KB, KIND, KS, 4) GB300_SEG_RNETWORK(KB, KIND, KS, 8)
+
 #define GB300_SEG_VALUES(KB, FP, FS, ...) GB300_SEG_RADIX(KB, FP, FS, 0) GB300_SEG_RADIX(KB, FP, FS, 4) GB300_SEG_RADIX(KB, FP, FS, 8)
 #define GB300_SEG_NET_VALUES(KB, KIND, KS) GB300_SEG_NETWORK(KB, KIND, KS, 0) GB300_SEG_NETWORK(KB, KIND, KS, 4) GB300_SEG_NETWORK(KB, KIND, KS, 8)

@@ -147,6 +147,10 @@ struct signed_of<8>
   using type = long long;
 };
 
+// Network kinds: 0 unsigned, 1 signed, 2 floating point (native comparisons, CUB's merge
+// networks); NET_RADIX + FP mode: radix order of the digit source (see RadixNetworkCompare).
+constexpr int NET_RADIX = 3;
+
 template <int KB, int KIND>
 struct NativeKey
 {
@@ -205,6 +209,34 @@ struct NetworkCompare
   {
     return descending ? NativeKey<KB, KIND>::less(b, a) : NativeKey<KB, KIND>::less(a, b);
   }
+  __device__ bool equal(U a, U b) const
+  {
+    return NativeKey<KB, KIND>::equal(a, b);
+  }
+};
+
+// Radix order for the networks (segmented radix sort, learned buckets): keys compare by the
+// bits [bit, bit + width) of their digit source, so a network sorts exactly as the radix
+// passes would. FP is the key mode of digit_source.
+template <int KB, int FP>
+struct RadixNetworkCompare
+{
+  using U = typename uint_of<KB>::type;
+  KeyCodec codec;
+  int bit;
+  U mask;
+  __device__ U key(U a) const
+  {
+    return U(digit_source<U, FP>(encode_key<U>(a, codec)) >> bit) & mask;
+  }
+  __device__ bool operator()(U a, U b) const
+  {
+    return key(a) < key(b);
+  }
+  __device__ bool equal(U a, U b) const
+  {
+    return key(a) == key(b);
+  }
 };
 
 // Bit pattern CUB loads past the end of a segment: the raw key that encodes to all ones
@@ -242,14 +274,15 @@ struct NetworkSmem
 };
 
 // One sub-warp sorts one segment of `size` keys at `kin` into `kout` (may alias).
-template <int KB, int KIND, int VB, int T, int I>
+template <int KB, int VB, int T, int I, class Cmp>
 __device__ __forceinline__ void network_sort_segment(
   const typename uint_of<KB>::type* kin,
   typename uint_of<KB>::type* kout,
   const typename value_word<VB>::type* vin,
   typename value_word<VB>::type* vout,
   int size,
-  bool descending,
+  const Cmp& op,
+  typename uint_of<KB>::type oob, // raw key past the end: compares after every key
   typename uint_of<KB>::type* kshared,
   typename value_word<VB>::type* vshared,
   uint32_t member_mask,
@@ -258,7 +291,6 @@ __device__ __forceinline__ void network_sort_segment(
   using U         = typename uint_of<KB>::type;
   using V         = typename value_word<VB>::type;
   constexpr int TILE = T * I;
-  const NetworkCompare<KB, KIND> op{descending};
 
   if (size < 3)
   {
@@ -283,7 +315,7 @@ __device__ __forceinline__ void network_sort_segment(
       {
         const U lhs       = kin[0];
         const U rhs       = kin[1];
-        const bool keep   = NativeKey<KB, KIND>::equal(lhs, rhs) || op(lhs, rhs);
+        const bool keep   = op.equal(lhs, rhs) || op(lhs, rhs);
         V lv{}, rv{};
         if constexpr (VB > 0)
         {
@@ -302,7 +334,6 @@ __device__ __forceinline__ void network_sort_segment(
     return;
   }
 
-  const U oob = network_oob<KB, KIND>(descending);
   U keys[I];
   V vals[VB > 0 ? I : 1];
 #pragma unroll
@@ -486,17 +517,26 @@ __device__ __forceinline__ void seg_network_body(const SegSortParams& p, const u
       const uint32_t s   = list[item];
       const long long b  = load_offset(p.begin_offsets, s, p.offsets_64);
       const int size     = int(load_offset(p.end_offsets, s, p.offsets_64) - b);
-      network_sort_segment<KB, KIND, VB, T, I>(
-        static_cast<const U*>(p.keys_in) + b,
-        static_cast<U*>(p.keys_out) + b,
-        VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
-        VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,
-        size,
-        p.descending != 0,
-        kshared,
-        vshared,
-        member_mask,
-        l);
+      const U* kin = static_cast<const U*>(p.keys_in) + b;
+      U* kout      = static_cast<U*>(p.keys_out) + b;
+      const V* vin = VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr;
+      V* vout      = VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr;
+      if constexpr (KIND >= NET_RADIX)
+      {
+        // radix order: ascending in the encoded key (the order lives in the codec); the key
+        // decoding from all ones sorts last
+        const int width = p.end_bit - p.begin_bit;
+        const RadixNetworkCompare<KB, KIND - NET_RADIX> op{
+          p.codec, p.begin_bit, width >= 8 * KB ? U(~U(0)) : U((U(1) << width) - 1)};
+        network_sort_segment<KB, VB, T, I>(
+          kin, kout, vin, vout, size, op, decode_key<U>(U(~U(0)), p.codec), kshared, vshared, member_mask, l);
+      }
+      else
+      {
+        const NetworkCompare<KB, KIND> op{p.descending != 0};
+        network_sort_segment<KB, VB, T, I>(
+          kin, kout, vin, vout, size, op, network_oob<KB, KIND>(p.descending != 0), kshared, vshared, member_mask, l);
+      }
     }
     __syncwarp();
   }

@@ -44,7 +44,9 @@ void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&na
     "gb300_seg_block_l_" + rad,
     "gb300_seg_hist_k" + std::to_string(kb) + "_" + fs,
     "gb300_seg_scan",
-    "gb300_seg_pass_" + rad};
+    "gb300_seg_pass_" + rad,
+    "gb300_seg_small_" + kv + "r" + fs,
+    "gb300_seg_medium_" + kv + "r" + fs};
   for (int i = 0; i < SK_COUNT; ++i)
   {
     std::snprintf(names[i], sizeof(names[i]), "%s", n[i].c_str());
@@ -67,6 +69,8 @@ SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
   p.pass_items          = seg_pass_items(kb, vb);
   p.network_small_smem  = seg_network_smem(kb, vb, p.small_threads, p.small_items);
   p.network_medium_smem = seg_network_smem(kb, vb, p.medium_threads, p.medium_items);
+  p.network_rsmall_smem  = seg_network_smem(kb, vb, SEG_RSMALL_THREADS, SEG_RSMALL_ITEMS);
+  p.network_rmedium_smem = seg_network_smem(kb, vb, SEG_RMEDIUM_THREADS, SEG_RMEDIUM_ITEMS);
   p.block_s_tpb         = seg_block_s_tpb(kb);
   p.block_l_tpb         = seg_block_l_tpb(kb);
   p.block_s_smem        = seg_block_smem(kb, seg_block_s_tpb(kb), seg_block_s_items(kb));
@@ -232,13 +236,13 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.begin_offsets   = c.begin_offsets;
     p.end_offsets     = c.end_offsets;
     p.offsets_64      = c.offsets_64;
-    p.partition       = !c.radix_only && nseg > uint64_t(SEG_PARTITION_THRESHOLD);
+    p.partition       = c.radix_only || nseg > uint64_t(SEG_PARTITION_THRESHOLD);
     p.num_segments    = nseg;
     p.num_items       = n;
     p.max_device_segments = max_dev;
     p.max_tiles       = max_tiles;
-    p.small_tile      = pol.small_threads * pol.small_items;
-    p.medium_tile     = c.radix_only ? 0 : pol.medium_threads * pol.medium_items; // no merge networks
+    p.small_tile      = c.radix_only ? SEG_RSMALL_THREADS * SEG_RSMALL_ITEMS : pol.small_threads * pol.small_items;
+    p.medium_tile     = c.radix_only ? SEG_RMEDIUM_THREADS * SEG_RMEDIUM_ITEMS : pol.medium_threads * pol.medium_items;
     p.block_small_cap = pol.block_s_cap;
     p.block_large_cap = pol.block_l_cap;
     p.device_tile     = uint32_t(pass_tile);
@@ -272,14 +276,18 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.codec         = codec;
     p.begin_bit     = begin_bit;
     p.end_bit       = end_bit;
-    if (!c.radix_only && nseg > uint64_t(SEG_PARTITION_THRESHOLD))
+    // radix order: the same networks comparing digit sources (every segment count)
+    const CUkernel small        = c.radix_only ? ks.k[SK_RSMALL] : ks.k[SK_SMALL];
+    const CUkernel medium       = c.radix_only ? ks.k[SK_RMEDIUM] : ks.k[SK_MEDIUM];
+    const uint64_t small_smem   = c.radix_only ? pol.network_rsmall_smem : pol.network_small_smem;
+    const uint64_t medium_smem  = c.radix_only ? pol.network_rmedium_smem : pol.network_medium_smem;
+    if (c.radix_only || nseg > uint64_t(SEG_PARTITION_THRESHOLD))
     {
-      launch("seg_small", ks.k[SK_SMALL], unsigned(sms * occupancy(ks.k[SK_SMALL], SEG_NETWORK_TPB, pol.network_small_smem)),
-             SEG_NETWORK_TPB, pol.network_small_smem, c.stream, p);
+      launch("seg_small", small, unsigned(sms * occupancy(small, SEG_NETWORK_TPB, small_smem)), SEG_NETWORK_TPB,
+             small_smem, c.stream, p);
     }
-    launch("seg_medium", ks.k[SK_MEDIUM],
-           unsigned(sms * occupancy(ks.k[SK_MEDIUM], SEG_NETWORK_TPB, pol.network_medium_smem)), SEG_NETWORK_TPB,
-           pol.network_medium_smem, c.stream, p);
+    launch("seg_medium", medium, unsigned(sms * occupancy(medium, SEG_NETWORK_TPB, medium_smem)), SEG_NETWORK_TPB,
+           medium_smem, c.stream, p);
     launch("seg_block_s", ks.k[SK_BLOCK_S], unsigned(sms * occupancy(ks.k[SK_BLOCK_S], pol.block_s_tpb, pol.block_s_smem)),
            unsigned(pol.block_s_tpb), pol.block_s_smem, c.stream, p);
     launch("seg_block_l", ks.k[SK_BLOCK_L], unsigned(sms * occupancy(ks.k[SK_BLOCK_L], pol.block_l_tpb, pol.block_l_smem)),

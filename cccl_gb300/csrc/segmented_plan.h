@@ -31,6 +31,8 @@ struct SegmentedPolicy
   int32_t pass_items;
   uint64_t network_small_smem;
   uint64_t network_medium_smem;
+  uint64_t network_rsmall_smem; // radix-order networks
+  uint64_t network_rmedium_smem;
   uint64_t block_s_smem;
   uint64_t block_l_smem;
   uint64_t pass_smem;
@@ -50,6 +52,8 @@ enum SegKernel : int
   SK_HIST,
   SK_SCAN,
   SK_PASS,
+  SK_RSMALL,  // the networks in radix order (segmented radix sort, learned buckets)
+  SK_RMEDIUM,
   SK_COUNT
 };
 

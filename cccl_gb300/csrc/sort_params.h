@@ -279,7 +279,8 @@ struct LearnedBoundsParams
   const void* keys; // partitioned (raw) keys: bucket ids are non-decreasing along them
   unsigned long long num_items;
   const LearnedModel* model;
-  unsigned long long* bounds; // [2^bucket_log2 + 1]: first index of every bucket, then n
+  unsigned long long* begins; // [2^bucket_log2], cleared: first index of every non-empty bucket
+  unsigned long long* ends;   // [2^bucket_log2], cleared: one past its last index
   KeyCodec codec;
   int bucket_log2;
   int pad0;

@@ -178,6 +178,13 @@ GB300_HD constexpr int seg_medium_items(int kb, int vb)
 }
 constexpr int SEG_PARTITION_THRESHOLD = 500; // dispatch_segmented_sort.cuh:465
 
+// The same networks in radix order (segmented radix sort, learned buckets) are not tied to
+// CUB's shapes: 8 lanes x 8 keys and a full warp x 8 keys.
+constexpr int SEG_RSMALL_THREADS  = 8;
+constexpr int SEG_RSMALL_ITEMS    = 8;
+constexpr int SEG_RMEDIUM_THREADS = 32;
+constexpr int SEG_RMEDIUM_ITEMS   = 8;
+
 // Block classes (free of the reference): one CTA sorts one segment in shared memory, by a
 // stable merge sort or by LSD radix passes; the algorithm and shape per key width come from
 // measurements on GB300 (the GB300_SEG_BLOCK_* macros override them in tuning builds).
@@ -305,9 +312,10 @@ GB300_HD constexpr size_t learned_pass_smem(int kb, int vb)
 }
 
 constexpr int LEARNED_FIT_TPB    = LEARNED_SAMPLE / LEARNED_LEAVES; // one sample point per thread
-constexpr int LEARNED_BOUNDS_TPB = 256;
 // Smallest input the learned path takes; below it the plain radix sort runs.
 constexpr unsigned long long LEARNED_MIN_ITEMS = 1ull << 20;
-// Target keys per bucket: the buckets' block sort holds up to 8192 keys.
+// Target keys per bucket: ~4096, the block sort class (two partition passes up to 2^28 keys).
+// 64-key buckets of 8-byte keys (one more partition pass, radix-order merge networks of 8 x 8
+// and 32 x 8 keys) measured slower on GB300: f64 + i64 at 2^30, 102 ms against 81 ms.
 constexpr int LEARNED_BUCKET_ITEMS_LOG2 = 12;
 } // namespace gb300

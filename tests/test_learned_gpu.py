@@ -22,7 +22,8 @@ def _lib(built_library):
     return built_library
 
 
-def _expected_buckets(n):
+def _expected_buckets(n, key_bytes):
+    """About 4096 keys per bucket, 2^8 to 2^24 buckets, whatever the key width."""
     b = min(max(int(np.ceil(np.log2(n))) - 12, 8), 24)
     return b, (b + 7) // 8
 
@@ -65,7 +66,7 @@ def test_skewed_floats_pairs(oracle, dtype, dist):
     k = I.with_specials(_skewed(dist, dtype, N, rng), rng, 1e-3)
     vtype = np.uint32 if np.dtype(dtype).itemsize == 4 else np.int64
     st = _check(oracle, k, I.index_values(N, vtype))
-    assert (st["bucket_log2"], st["partition_passes"]) == _expected_buckets(N)
+    assert (st["bucket_log2"], st["partition_passes"]) == _expected_buckets(N, np.dtype(dtype).itemsize)
 
 
 @pytest.mark.parametrize("dtype", [np.uint32, np.int32, np.float32, np.uint64, np.int64, np.float64],
