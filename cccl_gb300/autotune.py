@@ -33,10 +33,11 @@ TABLE = Path(__file__).resolve().parent / "tuning_gb300.json"
 CANDIDATES = {
     "onesweep": [
         "",
+        "-DGB300_PERSISTENT_TPB=1024 -DGB300_PERSISTENT_ITEMS=12",
+        "-DGB300_PERSISTENT_TPB=1024 -DGB300_PERSISTENT_ITEMS=14",
+        "-DGB300_PERSISTENT_TPB=896 -DGB300_PERSISTENT_ITEMS=16",
+        "-DGB300_PERSISTENT_TPB=768 -DGB300_PERSISTENT_ITEMS=24",
         "-DGB300_PERSISTENT_TPB=1024 -DGB300_PERSISTENT_ITEMS=6",
-        "-DGB300_PERSISTENT_TPB=768 -DGB300_PERSISTENT_ITEMS=8",
-        "-DGB300_PERSISTENT_TPB=512 -DGB300_PERSISTENT_ITEMS=8 -DGB300_PERSISTENT_MINB=2",
-        "-DGB300_PERSISTENT_TPB=512 -DGB300_PERSISTENT_ITEMS=16",
     ],
     "block": [
         "",

@@ -87,7 +87,7 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
   const uint64_t n = c.num_items;
   t.bucket_log2    = std::clamp(ceil_log2(n) - LEARNED_BUCKET_ITEMS_LOG2, 8, LEARNED_MAX_BUCKET_LOG2);
   t.passes         = (t.bucket_log2 + RADIX_BITS - 1) / RADIX_BITS;
-  t.tile_items     = uint64_t(s.pass_tpb) * s.pass_items;
+  t.tile_items     = persistent_tile_items(s.pass_tpb, s.pass_items);
   t.portion_items  = ((1ull << 30) - 1) / t.tile_items * t.tile_items; // 30-bit look-back counts
   t.num_portions   = ceil_div(n, t.portion_items);
   const uint64_t lookback_rows = ceil_div(n, t.tile_items) + t.num_portions;

@@ -14,13 +14,16 @@
 //   4. the staging tile is written out in order, so each digit's run lands contiguously;
 //      values follow the same permutation.
 //
-// Two kernels share this tile code:
+// Two kernels run these steps:
 //   * onesweep_persistent_body: the main path. One CTA per SM, launched cooperatively, walks
 //     tiles blockIdx.x, blockIdx.x + gridDim.x, ...; the next tile's keys and values are
 //     fetched into shared memory by a bulk async copy (cp.async.bulk + mbarrier) while the
-//     current tile is ranked and written, so HBM latency is off the critical path;
-//   * onesweep_body: CTA-per-tile with dynamic tile ids and plain warp-striped loads; used
-//     when the caller's buffers are not 16-byte aligned.
+//     current tile is ranked, so HBM latency is off the critical path. Its threads are
+//     split: 256 look-back threads run step 2 while the others rank, and a tile is written
+//     out one iteration after it was ranked, so the look-back latency is hidden as well;
+//   * onesweep_body (onesweep_tile): CTA-per-tile with dynamic tile ids and plain
+//     warp-striped loads; used when the caller's buffers are not 16-byte aligned, and by
+//     the segmented sort's device-class pass.
 #pragma once
 
 #include "sort_policy.h"
@@ -66,6 +69,53 @@ struct ComputedDigits
   uint8_t* stage; // [TILE] digit of every staging slot
 };
 
+// Decoupled look-back of digit d for `tile` (tile > 0): the sum of the predecessors'
+// counts back to the nearest inclusive prefix. BATCH predecessor rows are read per step (one
+// L2 round trip): inclusive prefixes spread from tile to tile at about BATCH tiles per round
+// trip, which bounds the pass's tile rate when every CTA waits for its walk. `failed` is set
+// when a predecessor reported an error or never published (bounded wait).
+template <int BATCH = LOOKBACK_BATCH>
+__device__ __forceinline__ uint32_t lookback_walk(const OnesweepParams& p, uint32_t tile, int d, bool& failed)
+{
+  const uint32_t* col = p.lookback + (size_t) p.tile_row_base * RADIX_DIGITS + d;
+  uint32_t excl       = 0;
+  bool done           = false;
+  failed              = false;
+  for (int j = int(tile) - 1; !done; j -= BATCH)
+  {
+    uint32_t w[BATCH];
+#pragma unroll
+    for (int k = 0; k < BATCH; ++k)
+    {
+      w[k] = (j - k >= 0) ? load_status(col + (size_t) (j - k) * RADIX_DIGITS) : LB_INCLUSIVE;
+    }
+#pragma unroll
+    for (int k = 0; k < BATCH; ++k)
+    {
+      if (!done)
+      {
+        uint32_t v = w[k];
+        if ((v & LB_FLAGS) == LB_EMPTY)
+        {
+          v = wait_status(col + (size_t) (j - k) * RADIX_DIGITS);
+        }
+        const uint32_t f = v & LB_FLAGS;
+        if (f == LB_ERROR)
+        {
+          failed = true;
+          done   = true;
+        }
+        else
+        {
+          excl += v & LB_VALUE;
+          done = (f == LB_INCLUSIVE);
+        }
+      }
+    }
+  }
+  return excl;
+}
+
 // Per-tile steps 1-4. Preconditions: whist is zero, keys[] hold the tile's encoded keys
 // (padding keys of a partial tile are all-ones), misc[1] says whether stores are
 // disabled. load_values(vals) is called once after the ranking to fill the values.
@@ -106,42 +156,39 @@ __device__ __forceinline__ void onesweep_tile(
   {
     warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
   }
+  if (STABLE && tid == 0)
+  {
+    if constexpr (Digits::computed)
+    {
+      misc[4] = dg.d[0];
+    }
+    else
+    {
+      misc[4] = extract_digit<U, FP>(keys[0], bit, dmask);
+    }
+  }
   __syncthreads();
 
   // ---- tile positions; publish the tile's digit counts; look-back ----
   if (tid < R)
   {
-    if (STABLE && tid < 32)
-    {
-      // Short circuit (the reference's TryShortCircuit, agent_radix_sort_onesweep.cuh:386-467):
-      // when every real key of the tile has the tile's first digit, the stable permutation is
-      // the identity and the keys go out straight from registers. misc[3] = flag | digit << 8;
-      // the barrier inside block_digit_offsets publishes it to warps 0-7, bar 2 to the rest.
-      uint32_t d0;
-      if constexpr (Digits::computed)
-      {
-        d0 = dg.d[0];
-      }
-      else
-      {
-        d0 = extract_digit<U, FP>(keys[0], bit, dmask);
-      }
-      d0         = __shfl_sync(0xffffffffu, d0, 0);
-      uint32_t c = 0;
-      for (int w = tid; w < NW; w += 32)
-      {
-        c += whist[w * R + d0];
-      }
-      c = __reduce_add_sync(0xffffffffu, c);
-      const uint32_t pad_digit = Digits::computed ? 255u : dmask;
-      const uint32_t real_d0   = c - (d0 == pad_digit ? uint32_t(TILE) - valid : 0u);
-      if (tid == 0)
-      {
-        misc[3] = real_d0 == valid ? (1u | (d0 << 8)) : 0u;
-      }
-    }
     uint32_t start;
     const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start);
+    if (STABLE)
+    {
+      // Short circuit (the reference's TryShortCircuit, agent_radix_sort_onesweep.cuh:386-467):
+      // when every real key of the tile has the first key's digit (padding keys carry the
+      // largest digit and are discounted), the stable permutation is the identity and the
+      // keys go out straight from registers. misc[3] = flag | digit << 8, written by that
+      // digit's thread; barrier 1 publishes it to warps 0-7, bar 2 to the rest.
+      if (uint32_t(tid) == misc[4])
+      {
+        const uint32_t pad_digit = Digits::computed ? 255u : dmask;
+        const uint32_t real      = total - (uint32_t(tid) == pad_digit ? uint32_t(TILE) - valid : 0u);
+        misc[3]                  = real == valid ? (1u | (uint32_t(tid) << 8)) : 0u;
+      }
+      named_barrier_256();
+    }
     uint32_t* lb_row     = p.lookback + (size_t) (p.tile_row_base + tile) * R;
     store_status(lb_row + tid, (tile == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
     asm volatile("bar.arrive 2, %0;" ::"n"(TPB) : "memory");
@@ -150,42 +197,7 @@ __device__ __forceinline__ void onesweep_tile(
     bool failed   = false;
     if (tile > 0)
     {
-      // Read LOOKBACK_BATCH predecessor rows per step: a sequential walk would cap the
-      // pass at one tile per L2 round trip.
-      const uint32_t* col = p.lookback + (size_t) p.tile_row_base * R + tid;
-      bool done           = false;
-      for (int j = int(tile) - 1; !done; j -= LOOKBACK_BATCH)
-      {
-        uint32_t w[LOOKBACK_BATCH];
-#pragma unroll
-        for (int k = 0; k < LOOKBACK_BATCH; ++k)
-        {
-          w[k] = (j - k >= 0) ? load_status(col + (size_t) (j - k) * R) : LB_INCLUSIVE;
-        }
-#pragma unroll
-        for (int k = 0; k < LOOKBACK_BATCH; ++k)
-        {
-          if (!done)
-          {
-            uint32_t v = w[k];
-            if ((v & LB_FLAGS) == LB_EMPTY)
-            {
-              v = wait_status(col + (size_t) (j - k) * R);
-            }
-            const uint32_t f = v & LB_FLAGS;
-            if (f == LB_ERROR)
-            {
-              failed = true;
-              done   = true;
-            }
-            else
-            {
-              excl += v & LB_VALUE;
-              done = (f == LB_INCLUSIVE);
-            }
-          }
-        }
-      }
+      excl = lookback_walk(p, tile, tid, failed);
       store_status(lb_row + tid, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
       if (failed)
       {
@@ -428,16 +440,35 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
-// Persistent kernel: tiles blockIdx.x + k * gridDim.x, the next tile prefetched into
-// shared memory by bulk async copies while the current one is processed.
+// Persistent kernel, warp-specialised and pipelined. The CTA has TPB - LOOKBACK_THREADS
+// "main" threads, whose tiles hold (TPB - LOOKBACK_THREADS) * ITEMS keys, and
+// LOOKBACK_THREADS = 256 look-back threads, one per digit. It walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...; iteration i (tile t_i, buffer i % 3):
+//
+//   main:      prefetch t_(i+1) | load t_i, count digits | BH | write out t_(i-1) after BG |
+//              BO | rank t_i, stage it in its own buffer | main barrier
+//   look-back: BH | tile positions, publish the tile's counts | BO | walk back, global
+//              offsets of t_i | BG
+//
+// The walk of t_i overlaps the ranking of t_i and the loading of t_(i+1); its result is
+// needed only when t_i is written out, one iteration later, so the look-back's L2 round
+// trips are off the critical path. Three tile buffers rotate: the input of t_(i+1) (bulk
+// copy in flight), the input and then the staging tile of t_i, the staging tile of t_(i-1)
+// (being written out).
+//
+// Named barriers: 1 the look-back threads' digit scan (256); 3 BH, 4 BO, 5 BG (all threads:
+// BH main arrive / look-back sync, BO both sync, BG look-back arrive / main sync); 6 main
+// threads only. BO is a sync on both sides, so the look-back threads cannot arrive at BG
+// for t_(i+1) before the main threads have consumed BG for t_i.
 // ---------------------------------------------------------------------------------------
 template <int KB, int VB, int TPB, int ITEMS, size_t EXTRA = 0>
 struct PersistentSmem
 {
   using U                   = typename uint_of<KB>::type;
   using V                   = typename value_word<VB>::type;
-  static constexpr int NW   = TPB / 32;
-  static constexpr int TILE = TPB * ITEMS;
+  static constexpr int MT   = TPB - LOOKBACK_THREADS; // main threads
+  static constexpr int NW   = MT / 32;                // main warps: one digit-counter row each
+  static constexpr int TILE = MT * ITEMS;
   static constexpr size_t whist_off  = 0;
   static constexpr size_t gdelta_off = whist_off + sizeof(uint32_t) * NW * RADIX_DIGITS;
   static constexpr size_t misc_off   = gdelta_off + sizeof(long long) * RADIX_DIGITS;
@@ -445,9 +476,13 @@ struct PersistentSmem
   static constexpr size_t kbytes     = ((sizeof(U) * TILE + 15) / 16) * 16;
   static constexpr size_t vbytes     = VB > 0 ? sizeof(V) * TILE : 0;
   static constexpr size_t buf_bytes  = kbytes + vbytes; // keys, then values; input and staging
-  static constexpr size_t extra_off  = buf_off + 2 * buf_bytes; // the pass hook's own region
+  static constexpr size_t extra_off  = buf_off + 3 * buf_bytes; // the pass hook's own region
   static constexpr size_t bytes      = extra_off + EXTRA;
+  static_assert(MT >= 32 && MT % 32 == 0, "whole main warps");
 };
+// misc words: [2] sticky failure of the CTA (its stores are disabled), [3] single-digit
+// flag and digit of the tile being ranked, [4] digit of the tile's first key, [8..15] scan
+// scratch, [16..21] three mbarriers.
 
 // Pass hook of the persistent kernel: the plain radix pass has none. A hook may fill its
 // shared-memory region once per CTA (setup) and supply computed digits per tile.
@@ -467,9 +502,13 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
   using L            = PersistentSmem<KB, VB, TPB, ITEMS, EXTRA>;
   using U            = typename L::U;
   using V            = typename L::V;
+  using Digits       = typename Hook::template digits_t<ITEMS>;
+  constexpr int MT   = L::MT;
   constexpr int NW   = L::NW;
   constexpr int R    = RADIX_DIGITS;
   constexpr int TILE = L::TILE;
+  static_assert(STABLE || VB == 0, "pairs need a stable pass");
+  static_assert(STABLE || !Digits::computed, "computed digits are ranked stably");
 
   extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
@@ -488,8 +527,9 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
     return;
   }
   const int tid         = threadIdx.x;
-  const int wofs        = (tid >> 5) * ITEMS * 32 + (tid & 31);
   const uint32_t ntiles = p.portion_tiles;
+  const int bit         = p.current_bit;
+  const uint32_t dmask  = (1u << p.num_bits) - 1u;
   // full tiles come by bulk copy; the partial last tile is read with plain loads
   const uint32_t nfull = p.portion_items / TILE;
   auto issue           = [&](uint32_t t, int b) {
@@ -505,6 +545,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
   {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
     mbar_init_fence();
     misc[2] = 0u;
     if (blockIdx.x < nfull)
@@ -512,91 +553,271 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
       issue(blockIdx.x, 0);
     }
   }
+  for (int i = tid; i < NW * R; i += TPB)
+  {
+    whist[i] = 0;
+  }
   hook.setup(smem + L::extra_off);
   __syncthreads();
 
-  uint32_t parity = 0; // bit b: phase parity to wait for on buffer b
-  int cur         = 0;
-  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x, cur ^= 1)
+  if (tid < MT)
   {
-    const uint32_t tn = t + gridDim.x;
-    if (tid == 0)
-    {
-      misc[1] = misc[2];
-      if (tn < nfull)
-      {
-        fence_proxy_async_smem(); // buffer cur^1 was last accessed by the generic proxy
-        issue(tn, cur ^ 1);
-      }
-    }
-    for (int i = tid; i < NW * R; i += TPB)
-    {
-      whist[i] = 0;
-    }
+    // ================================ main threads ================================
+    const int warp  = tid >> 5;
+    const int lane  = tid & 31;
+    const int wofs  = warp * ITEMS * 32 + lane;
+    U* kout         = static_cast<U*>(p.keys_out);
+    V* vout         = static_cast<V*>(p.values_out);
+    uint8_t* dstage = nullptr; // computed digits of the staged tile
 
-    U keys[ITEMS];
-    V vals[VB > 0 ? ITEMS : 1];
-    const uint32_t tile_first = t * TILE;
-    const uint32_t valid      = min(uint32_t(TILE), p.portion_items - tile_first);
-    bool data_ok              = true;
-    if (t < nfull)
-    {
-      data_ok = mbar_wait(&mbar[cur], (parity >> cur) & 1u);
-      parity ^= 1u << cur;
-      const U* ks = kbuf(cur);
+    // Consecutive staging slots of one digit go to consecutive outputs. Every store is
+    // bounds-checked against the output size, so even corrupted offsets (a look-back that
+    // gave up) cannot write outside the caller's buffers.
+    auto write_out = [&](int b, uint32_t valid) {
+      const U* ks                        = kbuf(b);
+      const V* vs                        = vbuf(b);
+      const bool full                    = valid == uint32_t(TILE);
+      const unsigned long long out_limit = misc[2] != 0u ? 0ull : p.num_items_total;
 #pragma unroll
-      for (int i = 0; i < ITEMS; ++i)
+      for (int j = 0; j < ITEMS; ++j)
       {
-        keys[i] = ks[wofs + i * 32];
+        const uint32_t s = j * MT + tid;
+        if (full || s < valid)
+        {
+          const U k = ks[s];
+          uint32_t d;
+          if constexpr (Digits::computed)
+          {
+            d = dstage[s];
+          }
+          else
+          {
+            d = extract_digit<U, FP>(k, bit, dmask);
+          }
+          const long long g = gdelta[d] + (long long) s;
+          if ((unsigned long long) g < out_limit)
+          {
+            __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+            if constexpr (VB > 0)
+            {
+              __stcs(vout + g, vs[s]);
+            }
+          }
+        }
       }
-      if (p.encode_in)
+    };
+
+    uint32_t parity     = 0; // bit b: phase parity to wait for on buffer b
+    int buf             = 0;
+    int prev_buf        = 0;
+    uint32_t prev_valid = 0;
+    bool have_prev      = false;
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+    {
+      const uint32_t tn = t + gridDim.x;
+      const int nbuf    = buf == 2 ? 0 : buf + 1;
+      if (tid == 0 && tn < nfull)
       {
+        fence_proxy_async_smem(); // buffer nbuf was last accessed by the generic proxy
+        issue(tn, nbuf);
+      }
+
+      // ---- load, count digits ----
+      U keys[ITEMS];
+      V vals[VB > 0 ? ITEMS : 1];
+      const uint32_t tile_first = t * TILE;
+      const uint32_t valid      = min(uint32_t(TILE), p.portion_items - tile_first);
+      if (t < nfull)
+      {
+        const bool data_ok = mbar_wait(&mbar[buf], (parity >> buf) & 1u);
+        parity ^= 1u << buf;
+        if (!data_ok)
+        {
+          // the copy never completed: this CTA stores nothing from here on
+          atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
+          misc[2] = 1u;
+        }
+        const U* ks = kbuf(buf);
 #pragma unroll
         for (int i = 0; i < ITEMS; ++i)
         {
-          keys[i] = encode_key<U>(keys[i], p.codec);
+          keys[i] = ks[wofs + i * 32];
         }
-      }
-      if constexpr (VB > 0)
-      {
-        const V* vs = vbuf(cur);
-#pragma unroll
-        for (int i = 0; i < ITEMS; ++i)
-        {
-          vals[i] = vs[wofs + i * 32];
-        }
-      }
-    }
-    else
-    {
-      load_tile_keys_global<KB, TPB, ITEMS>(p, tile_first, valid, keys);
-      if constexpr (VB > 0)
-      {
-        load_tile_values_global<VB, TPB, ITEMS>(p, tile_first, valid, vals);
-      }
-    }
-    typename Hook::template digits_t<ITEMS> dg;
-    hook.template compute<U, ITEMS>(keys, valid, wofs, dg, smem + L::extra_off);
-    if (!data_ok)
-    {
-      // the copy never completed: this CTA stores nothing from here on
-      atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
-      misc[2] = 1u;
-      misc[1] = 1u;
-    }
-    __syncthreads(); // whist zeroed, failure flags set, buffer cur consumed: it becomes the staging tile
-    onesweep_tile<KB, VB, FP, TPB, ITEMS, STABLE>(
-      p, t, valid, keys, whist, gdelta, misc, kbuf(cur), vbuf(cur), [&](auto& out) {
-        if constexpr (VB > 0)
+        if (p.encode_in)
         {
 #pragma unroll
           for (int i = 0; i < ITEMS; ++i)
           {
-            out[i] = vals[i];
+            keys[i] = encode_key<U>(keys[i], p.codec);
           }
         }
-      }, dg);
-    __syncthreads(); // staging tile written out; whist/gdelta/misc free for the next tile
+        if constexpr (VB > 0)
+        {
+          const V* vs = vbuf(buf);
+#pragma unroll
+          for (int i = 0; i < ITEMS; ++i)
+          {
+            vals[i] = vs[wofs + i * 32];
+          }
+        }
+      }
+      else
+      {
+        load_tile_keys_global<KB, MT, ITEMS>(p, tile_first, valid, keys);
+        if constexpr (VB > 0)
+        {
+          load_tile_values_global<VB, MT, ITEMS>(p, tile_first, valid, vals);
+        }
+      }
+      Digits dg;
+      hook.template compute<U, ITEMS>(keys, valid, wofs, dg, smem + L::extra_off);
+      if constexpr (Digits::computed)
+      {
+        warp_histogram_digits<ITEMS>(dg.d, whist + warp * R);
+        dstage = dg.stage;
+      }
+      else
+      {
+        warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+      }
+      if (tid == 0)
+      {
+        if constexpr (Digits::computed)
+        {
+          misc[4] = dg.d[0];
+        }
+        else
+        {
+          misc[4] = extract_digit<U, FP>(keys[0], bit, dmask);
+        }
+      }
+      asm volatile("bar.arrive 3, %0;" ::"n"(TPB) : "memory"); // BH: counts of t ready
+
+      // ---- the previous tile goes out while the look-back threads turn t's counts into positions ----
+      if (have_prev)
+      {
+        asm volatile("bar.sync 5, %0;" ::"n"(TPB) : "memory"); // BG: offsets of the previous tile
+        write_out(prev_buf, prev_valid);
+      }
+      asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO: positions of t in whist
+
+      // ---- rank t, stage it in its own buffer ----
+      const uint32_t single = STABLE ? misc[3] : 0u;
+      uint32_t pos[ITEMS];
+      if (single != 0u)
+      {
+        // one digit (the reference's TryShortCircuit, agent_radix_sort_onesweep.cuh:386-467):
+        // the stable permutation is the identity
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          pos[i] = uint32_t(wofs + i * 32);
+        }
+      }
+      else
+      {
+        __syncwarp();
+        if constexpr (Digits::computed)
+        {
+          warp_rank_stable_digits<ITEMS>(dg.d, pos, whist + warp * R);
+        }
+        else if constexpr (STABLE)
+        {
+          warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+        }
+        else
+        {
+          warp_rank_unstable_tail<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask, wofs, valid);
+        }
+      }
+      U* ks = kbuf(buf);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        ks[pos[i]] = keys[i];
+      }
+      if constexpr (Digits::computed)
+      {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          dg.stage[pos[i]] = uint8_t(dg.d[i]);
+        }
+      }
+      if constexpr (VB > 0)
+      {
+        V* vs = vbuf(buf);
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          vs[pos[i]] = vals[i];
+        }
+      }
+      __syncwarp(); // the warp's ranking atomics are done: clear its counter row for the next tile
+      for (int k = lane; k < R; k += 32)
+      {
+        whist[warp * R + k] = 0u;
+      }
+      // staging of t visible to every main thread; the previous tile's buffer is free for
+      // the next prefetch
+      asm volatile("bar.sync 6, %0;" ::"n"(MT) : "memory");
+      prev_buf   = buf;
+      prev_valid = valid;
+      have_prev  = true;
+      buf        = nbuf;
+    }
+    if (have_prev)
+    {
+      asm volatile("bar.sync 5, %0;" ::"n"(TPB) : "memory"); // BG of the last tile
+      write_out(prev_buf, prev_valid);
+    }
+  }
+  else
+  {
+    // ============================== look-back threads ==============================
+    const int d = tid - MT; // this thread's digit
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+    {
+      const uint32_t valid = min(uint32_t(TILE), p.portion_items - t * TILE);
+      asm volatile("bar.sync 3, %0;" ::"n"(TPB) : "memory"); // BH
+      uint32_t start;
+      const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start, d);
+      if (STABLE && uint32_t(d) == misc[4])
+      {
+        // every real key of the tile has the first key's digit (padding keys carry the
+        // largest digit and are discounted)
+        const uint32_t pad_digit = Digits::computed ? 255u : dmask;
+        const uint32_t real      = total - (uint32_t(d) == pad_digit ? uint32_t(TILE) - valid : 0u);
+        misc[3]                  = real == valid ? (1u | (uint32_t(d) << 8)) : 0u;
+      }
+      uint32_t* lb_row = p.lookback + (size_t) (p.tile_row_base + t) * R;
+      store_status(lb_row + d, (t == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+      asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO
+
+      uint32_t excl = 0;
+      if (t > 0)
+      {
+        bool failed = false;
+        excl        = lookback_walk<PERSISTENT_LOOKBACK_BATCH>(p, t, d, failed);
+        store_status(lb_row + d, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+        if (failed)
+        {
+          atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
+          misc[2] = 1u;
+        }
+      }
+      if (p.lookback_next != nullptr)
+      {
+        p.lookback_next[(size_t) (p.tile_row_base + t) * R + d] = 0u;
+      }
+      const unsigned long long base = p.bins[d] + excl;
+      gdelta[d]                     = (long long) base - (long long) start;
+      if (p.bins_next != nullptr && t == p.portion_tiles - 1)
+      {
+        p.bins_next[d] = base + total;
+      }
+      asm volatile("bar.arrive 5, %0;" ::"n"(TPB) : "memory"); // BG
+    }
   }
 }
 

@@ -61,7 +61,7 @@ plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, 
 {
   RadixTempPlan t{};
   t.num_passes    = int(ceil_div(uint64_t(end_bit - begin_bit), RADIX_BITS));
-  t.tile_items    = persistent ? uint64_t(pol.persistent_tpb) * pol.persistent_items
+  t.tile_items    = persistent ? persistent_tile_items(pol.persistent_tpb, pol.persistent_items)
                                : uint64_t(pol.onesweep_tpb) * pol.onesweep_items;
   // Look-back words carry a 30-bit count, so one launch covers < 2^30 keys.
   t.portion_items = ((1ull << 30) - 1) / t.tile_items * t.tile_items;
@@ -69,7 +69,7 @@ plan_radix_temp(const RadixPolicy& pol, uint64_t n, int begin_bit, int end_bit, 
   t.total_tiles   = ceil_div(n, t.tile_items);
   // Look-back rows are sized for the smaller tile of the two pass kernels, so the size a
   // caller queried is enough whichever kernel the buffers' alignment selects.
-  const uint64_t min_tile = std::min<uint64_t>(uint64_t(pol.persistent_tpb) * pol.persistent_items,
+  const uint64_t min_tile = std::min<uint64_t>(persistent_tile_items(pol.persistent_tpb, pol.persistent_items),
                                                uint64_t(pol.onesweep_tpb) * pol.onesweep_items);
   const uint64_t lookback_rows = ceil_div(n, min_tile) + t.num_portions;
 

@@ -29,16 +29,29 @@ constexpr int ONESWEEP_TPB     = 384; // CTA-per-tile fallback kernel
 #endif
 constexpr int PERSISTENT_MINB = GB300_PERSISTENT_MINB; // CTAs per SM the registers are sized for
 
-// Threads per CTA of the persistent kernel. Tuned on GB300 (2^28 keys): pairs run best
-// with 32 warps of 8 items (more warps hide the ranking latency), keys-only with 16 warps
-// of 20 items (bigger tiles per CTA barrier).
+// Threads per CTA of the persistent kernel: LOOKBACK_THREADS look-back threads (one per
+// digit) plus the main threads that load, rank and write the tiles. Measured on GB300 with
+// the autotuner (2^26 keys, one sort): keys-only runs best with 24 main warps of 14 items,
+// pairs with 20 main warps and as many items as three tile buffers leave room for (the
+// ranking is latency-bound, so more warps per SM pay until the registers run out).
+constexpr int LOOKBACK_THREADS = 256;
 GB300_HD constexpr int persistent_tpb(int kb, int vb)
 {
 #ifdef GB300_PERSISTENT_TPB
   return (void) kb, (void) vb, GB300_PERSISTENT_TPB;
 #else
-  return (void) kb, vb > 0 ? 1024 : 512;
+  return (void) kb, vb > 0 ? 896 : 1024;
 #endif
+}
+// Predecessor rows the persistent kernel's look-back threads read per step: they have no
+// other work, so they can keep more loads in flight than the CTA-per-tile kernel's.
+#ifndef GB300_PERSISTENT_LOOKBACK_BATCH
+#  define GB300_PERSISTENT_LOOKBACK_BATCH 8
+#endif
+constexpr int PERSISTENT_LOOKBACK_BATCH = GB300_PERSISTENT_LOOKBACK_BATCH;
+GB300_HD constexpr int persistent_main(int kb, int vb)
+{
+  return persistent_tpb(kb, vb) - LOOKBACK_THREADS;
 }
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
@@ -77,22 +90,22 @@ GB300_HD constexpr size_t onesweep_smem_bytes(int kb, int vb)
        + (vb > 0 ? value_word_bytes(vb) * ONESWEEP_TPB * onesweep_items(kb, vb) : 0);
 }
 
-// Items per thread of the persistent onesweep kernel: the two tile buffers (keys + values)
-// must fit the 227 KB of shared memory next to the 16 KB of per-warp counters.
+// Items per main thread of the persistent onesweep kernel: the three tile buffers (keys +
+// values) must fit the 227 KB of shared memory next to the per-warp counters.
 GB300_HD constexpr int persistent_items_nominal(int kb, int vb)
 {
 #ifdef GB300_PERSISTENT_ITEMS
   return (void) kb, (void) vb, GB300_PERSISTENT_ITEMS;
 #else
-  return vb > 0 ? 8 : kb == 8 ? 16 : kb == 4 ? 20 : 24;
+  return vb > 0 ? 16 : kb == 8 ? 12 : kb == 4 ? 14 : 16;
 #endif
 }
 
 GB300_HD constexpr size_t persistent_smem_for(int kb, int vb, int items)
 {
-  return size_t(4) * (persistent_tpb(kb, vb) / 32) * 256 + size_t(8) * 256 + 128
-       + 2 * (round16(size_t(kb) * persistent_tpb(kb, vb) * items)
-              + (vb > 0 ? value_word_bytes(vb) * persistent_tpb(kb, vb) * items : 0));
+  return size_t(4) * (persistent_main(kb, vb) / 32) * 256 + size_t(8) * 256 + 128
+       + 3 * (round16(size_t(kb) * persistent_main(kb, vb) * items)
+              + (vb > 0 ? value_word_bytes(vb) * persistent_main(kb, vb) * items : 0));
 }
 
 // Nominal items, reduced until PERSISTENT_MINB CTAs fit in 227 KB of shared memory.
@@ -109,6 +122,12 @@ GB300_HD constexpr int persistent_items(int kb, int vb)
 GB300_HD constexpr size_t persistent_smem_bytes(int kb, int vb)
 {
   return persistent_smem_for(kb, vb, persistent_items(kb, vb));
+}
+
+// Keys per tile of the persistent kernel.
+GB300_HD constexpr unsigned long long persistent_tile_items(int tpb, int items)
+{
+  return (unsigned long long) (tpb - LOOKBACK_THREADS) * items;
 }
 
 GB300_HD constexpr int single_tile_capacity()
@@ -291,7 +310,7 @@ GB300_HD constexpr size_t learned_tables_bytes()
 
 GB300_HD constexpr size_t learned_extra_bytes(int kb, int vb, int items)
 {
-  return (void) kb, learned_tables_bytes() + round16(size_t(persistent_tpb(kb, vb)) * items);
+  return (void) kb, learned_tables_bytes() + round16(size_t(persistent_main(kb, vb)) * items);
 }
 
 GB300_HD constexpr int learned_items(int kb, int vb)

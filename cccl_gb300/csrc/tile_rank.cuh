@@ -33,13 +33,13 @@ __device__ __forceinline__ uint32_t lanemask_le()
   return m;
 }
 
-// Exclusive prefix over the 256 digit slots held by threads [0, 256) (one value per
-// thread). `scratch` holds 8 words. Must be called by exactly threads [0, 256).
-__device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch)
+// Exclusive prefix over the 256 digit slots held by one group of 256 threads (eight whole
+// warps; thread d holds digit d's value). `scratch` holds 8 words. Must be called by
+// exactly that group, and by no other thread of the CTA at the same time (named barrier 1).
+__device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch, int d = threadIdx.x)
 {
-  const int tid  = threadIdx.x;
-  const int lane = tid & 31;
-  const int w    = tid >> 5;
+  const int lane = d & 31;
+  const int w    = d >> 5;
   uint32_t x     = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1)
@@ -99,13 +99,13 @@ __device__ __forceinline__ void warp_histogram(const U (&keys)[ITEMS], uint32_t*
   }
 }
 
-// Threads [0, 256): turns per-warp counts whist[w][d] into tile positions (exclusive over
-// digits, then over warps). Returns this thread's digit total; *tile_start receives the
-// digit's first position in the tile.
+// One group of 256 threads (thread d, digit d): turns per-warp counts whist[w][d] into
+// tile positions (exclusive over digits, then over warps). Returns this thread's digit
+// total; *tile_start receives the digit's first position in the tile.
 template <int NW>
-__device__ __forceinline__ uint32_t block_digit_offsets(uint32_t* whist, uint32_t* scratch8, uint32_t* tile_start)
+__device__ __forceinline__ uint32_t
+block_digit_offsets(uint32_t* whist, uint32_t* scratch8, uint32_t* tile_start, int d = threadIdx.x)
 {
-  const int d    = threadIdx.x;
   uint32_t total = 0;
 #pragma unroll
   for (int w = 0; w < NW; ++w)
@@ -114,7 +114,7 @@ __device__ __forceinline__ uint32_t block_digit_offsets(uint32_t* whist, uint32_
     whist[w * RADIX_DIGITS + d] = total;
     total += c;
   }
-  const uint32_t start = digit_exclusive_scan(total, scratch8);
+  const uint32_t start = digit_exclusive_scan(total, scratch8, d);
 #pragma unroll
   for (int w = 0; w < NW; ++w)
   {
@@ -194,6 +194,22 @@ __device__ __forceinline__ void warp_rank_unstable(
   for (int i = 0; i < ITEMS; ++i)
   {
     pos[i] = atomicAdd(&whist_w[extract_digit<U, FP>(keys[i], bit, dmask)], 1u);
+  }
+}
+
+// Order-free tile positions for a tile whose keys at segment indexes >= valid are padding:
+// real keys take their digit's slots, padding keys the slots [valid, TILE) at their own
+// index. Padding keys carry the largest digit and come last in source order, so the
+// real keys of that digit fill exactly its slots below `valid`.
+template <class U, int FP, int ITEMS>
+__device__ __forceinline__ void warp_rank_unstable_tail(
+  const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask, int wofs, uint32_t valid)
+{
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t idx = uint32_t(wofs + i * 32);
+    pos[i] = idx < valid ? atomicAdd(&whist_w[extract_digit<U, FP>(keys[i], bit, dmask)], 1u) : idx;
   }
 }
 
