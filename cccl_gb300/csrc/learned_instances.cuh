@@ -22,6 +22,16 @@ extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitPa
     gb300::learned_pass_body<KB, VB, FP>(p);                                                                    \
   }
 
+// bucket sort kernels: CAP keys at most per bucket
+#define GB300_LEARNED_BUCKET(KB, VB, FP, FS, CAP)                                                                 \
+  static_assert(gb300::LearnedBucketSmem<KB, VB, CAP>::bytes == gb300::learned_bucket_smem(KB, VB, CAP),         \
+                "learned bucket shared-memory layout mismatch");                                                \
+  extern "C" __global__ void __launch_bounds__(gb300::learned_bucket_tpb(CAP), 65536 / 64 / gb300::learned_bucket_tpb(CAP)) \
+    gb300_learned_bucket##CAP##_k##KB##_v##VB##_##FS(const gb300::LearnedBucketParams p)                        \
+  {                                                                                                             \
+    gb300::learned_bucket_body<KB, VB, FP, gb300::learned_bucket_tpb(CAP), CAP>(p);                             \
+  }
+
 #define GB300_LEARNED(KB, FP, FS)                                                                                 \
   extern "C" __global__ void __launch_bounds__(256) gb300_learned_sample_k##KB##_##FS(                          \
     const gb300::LearnedSampleParams p)                                                                         \
@@ -40,7 +50,13 @@ extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitPa
   }                                                                                                             \
   GB300_LEARNED_PASS(KB, 0, FP, FS)                                                                             \
   GB300_LEARNED_PASS(KB, 4, FP, FS)                                                                             \
-  GB300_LEARNED_PASS(KB, 8, FP, FS)
+  GB300_LEARNED_PASS(KB, 8, FP, FS)                                                                             \
+  GB300_LEARNED_BUCKET(KB, 0, FP, FS, 8192)                                                                  \
+  GB300_LEARNED_BUCKET(KB, 4, FP, FS, 8192)                                                                  \
+  GB300_LEARNED_BUCKET(KB, 8, FP, FS, 8192)                                                                  \
+  GB300_LEARNED_BUCKET(KB, 0, FP, FS, 4096)                                                                  \
+  GB300_LEARNED_BUCKET(KB, 4, FP, FS, 4096)                                                                  \
+  GB300_LEARNED_BUCKET(KB, 8, FP, FS, 4096)
 
 #define GB300_LEARNED_FIT(KB)                                                                                     \
   extern "C" __global__ void __launch_bounds__(gb300::LEARNED_FIT_TPB) gb300_learned_fit_k##KB(                 \

@@ -403,4 +403,371 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// bucket sort: per bucket of n <= CAP keys, one counting pass on the top varying bits of
+// the ordering key t = digit_source(encode(key)) with 2^ceil(log2 n) bins, then the keys of
+// every bin ordered by (t, index in the bucket). Since t - min is split by its top bits,
+// bin order is t order; ranking a key among its bin by (t, index) makes the whole stable.
+// The partition passes keep equal keys in input order, so the index in the bucket is the
+// tie-break the plain sort uses. A bucket whose largest bin holds more than RUN_MAX keys
+// is left to the segmented radix sort (rest_ends[b] = ends[b]).
+//
+// Every thread keeps its PER keys and values in registers from load to the final placement
+// (all loads of a bucket precede all of its stores, so the output may alias the input);
+// shared memory holds the keys for the comparisons, the bins (start | count << 16 after
+// the scan) and, for bins of two or more keys, their members' indices. The sorted bucket
+// is assembled in shared memory and stored with coalesced writes: scattered 4- and 8-byte
+// stores cost one L1 transaction each and were the kernel's bottleneck.
+// ---------------------------------------------------------------------------------------
+template <int KB, int VB, int FP, int TPB, int CAP>
+__device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p)
+{
+  using U            = typename uint_of<KB>::type;
+  using V            = typename value_word<VB>::type;
+  using L            = LearnedBucketSmem<KB, VB, CAP>;
+  constexpr int NW   = TPB / 32;
+  constexpr int PER  = CAP / TPB; // keys per thread
+  static_assert(CAP % TPB == 0 && CAP < 65536, "16-bit bin fields and indices");
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  U* kraw        = reinterpret_cast<U*>(smem + L::kraw_off);
+  V* vst         = reinterpret_cast<V*>(smem + L::vst_off);
+  uint32_t* bins = reinterpret_cast<uint32_t*>(smem + L::bins_off);
+  uint16_t* perm = reinterpret_cast<uint16_t*>(smem + L::perm_off);
+  static_assert(NW <= 32, "one warp combines the per-warp values");
+  __shared__ unsigned long long range[2]; // min and max ordering key of the bucket
+  __shared__ uint32_t scan_w[NW], run_w[NW];
+  __shared__ unsigned long long bucket[3]; // id, begin, end
+
+  const int tid  = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const U* kin   = static_cast<const U*>(p.keys_in);
+  const V* vin   = static_cast<const V*>(p.values_in);
+  U* kout        = static_cast<U*>(p.keys_out);
+  V* vout        = static_cast<V*>(p.values_out);
+  auto key_of    = [&](U k) {
+    return digit_source<U, FP>(encode_key<U>(k, p.codec));
+  };
+
+  // Thread 0 takes the next bucket's ticket and bounds while the current one is sorted, and
+  // has the bulk-copy unit prefetch its keys and values into L2.
+  uint32_t nb_id              = 0;
+  unsigned long long nb_begin = 0, nb_end = 0;
+  auto fetch_next             = [&]() {
+    nb_id    = atomicAdd(p.counters, 1u);
+    nb_begin = nb_id < p.num_buckets ? p.begins[nb_id] : 0ull;
+    nb_end   = nb_id < p.num_buckets ? p.ends[nb_id] : 0ull;
+    if (nb_end > nb_begin && nb_end - nb_begin <= (unsigned long long) CAP)
+    {
+      // 16-byte aligned sub-range inside the arrays (which start 16-byte aligned)
+      const unsigned long long kb0 = (nb_begin * KB) & ~15ull;
+      const unsigned long long kb1 = min(nb_end * KB + 15, p.num_items * KB) & ~15ull;
+      if (kb1 > kb0)
+      {
+        bulk_prefetch_l2(static_cast<const unsigned char*>(p.keys_in) + kb0, uint32_t(kb1 - kb0));
+      }
+      if constexpr (VB > 0)
+      {
+        const unsigned long long vb0 = (nb_begin * VB) & ~15ull;
+        const unsigned long long vb1 = min(nb_end * VB + 15, p.num_items * VB) & ~15ull;
+        if (vb1 > vb0)
+        {
+          bulk_prefetch_l2(static_cast<const unsigned char*>(p.values_in) + vb0, uint32_t(vb1 - vb0));
+        }
+      }
+    }
+  };
+  if (tid == 0)
+  {
+    fetch_next();
+  }
+  while (true)
+  {
+    if (tid == 0)
+    {
+      bucket[0] = nb_id;
+      bucket[1] = nb_begin;
+      bucket[2] = nb_end;
+      range[0]  = ~0ull;
+      range[1]  = 0ull;
+    }
+    __syncthreads();
+    const uint32_t b             = uint32_t(bucket[0]);
+    const unsigned long long beg = bucket[1];
+    const unsigned long long end = bucket[2];
+    if (b >= p.num_buckets)
+    {
+      break;
+    }
+    if (tid == 0)
+    {
+      fetch_next();
+    }
+    const uint32_t n = end > beg ? uint32_t(min(end - beg, (unsigned long long) CAP + 1)) : 0u;
+    if (n <= 1 || n > uint32_t(CAP))
+    {
+      // empty and single-key buckets need no ordering; large ones go to the segmented sort
+      if (tid == 0)
+      {
+        p.rest_ends[b] = n > uint32_t(CAP) ? end : beg;
+        if (n == 1 && p.keys_out != p.keys_in)
+        {
+          kout[beg] = kin[beg];
+          if constexpr (VB > 0)
+          {
+            vout[beg] = vin[beg];
+          }
+        }
+      }
+      __syncthreads(); // bucket[] is read by everyone before thread 0 takes the next ticket
+      continue;
+    }
+    const int s       = 32 - __clz(n - 1); // bins = 2^s >= n
+    const uint32_t nb = 1u << s;
+
+    // ---- load (registers and shared memory); clear the bins; range of the ordering keys ----
+    U kr[PER];
+    V vr[VB > 0 ? PER : 1];
+#pragma unroll
+    for (int j = 0; j < PER; ++j)
+    {
+      const uint32_t i = tid + j * TPB;
+      kr[j]            = i < n ? kin[beg + i] : U(0);
+    }
+    if constexpr (VB > 0)
+    {
+#pragma unroll
+      for (int j = 0; j < PER; ++j)
+      {
+        const uint32_t i = tid + j * TPB;
+        vr[j]            = i < n ? vin[beg + i] : V(0);
+      }
+    }
+    for (uint32_t i = tid; i < nb; i += TPB)
+    {
+      bins[i] = 0u;
+    }
+    U lo = U(~U(0)), hi = U(0);
+#pragma unroll
+    for (int j = 0; j < PER; ++j)
+    {
+      const uint32_t i = tid + j * TPB;
+      if (i < n)
+      {
+        kraw[i]   = kr[j];
+        const U t = key_of(kr[j]);
+        lo        = t < lo ? t : lo;
+        hi        = t > hi ? t : hi;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1)
+    {
+      const U a = __shfl_xor_sync(0xffffffffu, lo, o);
+      const U c = __shfl_xor_sync(0xffffffffu, hi, o);
+      lo        = a < lo ? a : lo;
+      hi        = c > hi ? c : hi;
+    }
+    if (lane == 0)
+    {
+      atomicMin(&range[0], (unsigned long long) lo);
+      atomicMax(&range[1], (unsigned long long) hi);
+    }
+    __syncthreads();
+    lo = U(range[0]);
+    hi = U(range[1]);
+
+    bool sorted_here = true;
+    if (lo == hi)
+    {
+      // one ordering key: input order is the stable order
+#pragma unroll
+      for (int j = 0; j < PER; ++j)
+      {
+        const uint32_t i = tid + j * TPB;
+        if (i < n)
+        {
+          kout[beg + i] = kr[j];
+          if constexpr (VB > 0)
+          {
+            vout[beg + i] = vr[j];
+          }
+        }
+      }
+    }
+    else
+    {
+      const U width   = U(hi - lo);
+      const int wbits = KB == 8 ? 64 - __clzll((long long) width) : 32 - __clz(uint32_t(width));
+      const int shift = wbits > s ? wbits - s : 0;
+      uint32_t sub[PER];
+#pragma unroll
+      for (int j = 0; j < PER; ++j)
+      {
+        sub[j] = uint32_t(U(key_of(kr[j]) - lo) >> shift);
+        if (tid + j * TPB < n)
+        {
+          atomicAdd(&bins[sub[j]], 1u);
+        }
+      }
+      __syncthreads();
+      // longest run; exclusive scan of the bins (thread t owns bins [t*per, (t+1)*per))
+      const uint32_t per   = (nb + TPB - 1) / TPB;
+      const uint32_t first = tid * per;
+      uint32_t run = 0, sum = 0;
+      for (uint32_t j = 0; j < per; ++j)
+      {
+        if (first + j < nb)
+        {
+          const uint32_t c = bins[first + j];
+          run              = c > run ? c : run;
+          sum += c;
+        }
+      }
+      uint32_t x = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+      {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+        {
+          x += y;
+        }
+      }
+      run = __reduce_max_sync(0xffffffffu, run);
+      if (lane == 31)
+      {
+        scan_w[warp] = x;
+        run_w[warp]  = run;
+      }
+      __syncthreads();
+      // every warp combines the warp totals itself: lane l holds warp l's
+      const uint32_t tw = lane < NW ? scan_w[lane] : 0u;
+      uint32_t pw       = tw;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+      {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, pw, o);
+        if (lane >= o)
+        {
+          pw += y;
+        }
+      }
+      const uint32_t base    = __shfl_sync(0xffffffffu, pw - tw, warp);
+      const uint32_t longest = __reduce_max_sync(0xffffffffu, lane < NW ? run_w[lane] : 0u);
+      if (longest > uint32_t(LEARNED_RUN_MAX))
+      {
+        sorted_here = false; // uniform across the CTA
+      }
+      else
+      {
+        // bins[x] = start | count << 16
+        uint32_t acc = base + x - sum;
+        for (uint32_t j = 0; j < per; ++j)
+        {
+          if (first + j < nb)
+          {
+            const uint32_t c = bins[first + j];
+            bins[first + j]  = acc | (c << 16);
+            acc += c;
+          }
+        }
+        __syncthreads();
+        // a key alone in its bin is placed; the others take a member slot of their bin (the
+        // start field counts up; the count field is unchanged)
+        uint32_t pos[PER];
+#pragma unroll
+        for (int j = 0; j < PER; ++j)
+        {
+          const uint32_t i = tid + j * TPB;
+          pos[j]           = 0xffffffffu;
+          if (i < n)
+          {
+            const uint32_t w = bins[sub[j]];
+            if ((w >> 16) == 1u)
+            {
+              pos[j] = w & 0xffffu;
+            }
+            else
+            {
+              perm[atomicAdd(&bins[sub[j]], 1u) & 0xffffu] = uint16_t(i);
+            }
+          }
+        }
+        __syncthreads();
+        // rank the others among their bin's members by (t, index); bins[x] = end | count << 16
+#pragma unroll
+        for (int j = 0; j < PER; ++j)
+        {
+          const uint32_t i = tid + j * TPB;
+          if (i < n && pos[j] == 0xffffffffu)
+          {
+            const uint32_t w  = bins[sub[j]];
+            const uint32_t b1 = w & 0xffffu;
+            const uint32_t b0 = b1 - (w >> 16);
+            uint32_t rank     = 0;
+            if (shift == 0)
+            {
+              // a bin holds one ordering key: the index alone decides
+              for (uint32_t r = b0; r < b1; ++r)
+              {
+                rank += perm[r] < i ? 1u : 0u;
+              }
+            }
+            else
+            {
+              const U ti = key_of(kr[j]);
+              for (uint32_t r = b0; r < b1; ++r)
+              {
+                const uint32_t m = perm[r];
+                const U tm       = key_of(kraw[m]);
+                rank += (tm < ti || (tm == ti && m < i)) ? 1u : 0u;
+              }
+            }
+            pos[j] = b0 + rank;
+          }
+        }
+        __syncthreads(); // every comparison read of kraw is done
+        // sorted order in shared memory, then coalesced stores
+#pragma unroll
+        for (int j = 0; j < PER; ++j)
+        {
+          if (tid + j * TPB < n)
+          {
+            kraw[pos[j]] = kr[j];
+            if constexpr (VB > 0)
+            {
+              vst[pos[j]] = vr[j];
+            }
+          }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER; ++j)
+        {
+          const uint32_t q = tid + j * TPB;
+          if (q < n)
+          {
+            kout[beg + q] = kraw[q];
+            if constexpr (VB > 0)
+            {
+              vout[beg + q] = vst[q];
+            }
+          }
+        }
+      }
+    }
+    if (tid == 0)
+    {
+      p.rest_ends[b] = sorted_here ? beg : end;
+      if (sorted_here)
+      {
+        atomicAdd(p.counters + 1, 1u);
+      }
+    }
+    __syncthreads(); // shared buffers and bucket[] free for the next bucket
+  }
+}
+
 } // namespace gb300

@@ -4,8 +4,8 @@
 // the same result and the same DoubleBuffer selector as the plain sort
 // (cub/cub/device/dispatch/dispatch_radix_sort.cuh:1698-1948 leaves the result of a
 // full-width sort of k-byte keys after k 8-bit passes, i.e. in the current buffer when k is
-// even). Bucket count: about 2^LEARNED_BUCKET_ITEMS_LOG2 keys per bucket (the block sort
-// classes of the segmented sort); the partition needs
+// even). Bucket count: about 2^learned_bucket_items_log2 keys per bucket (2048 or 4096, sorted
+// in shared memory); the partition needs
 // ceil(log2(buckets) / 8) stable passes.
 #include "learned_plan.h"
 
@@ -85,7 +85,9 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
     return t;
   }
   const uint64_t n = c.num_items;
-  t.bucket_log2    = std::clamp(ceil_log2(n) - LEARNED_BUCKET_ITEMS_LOG2, 8, LEARNED_MAX_BUCKET_LOG2);
+  const int items_log2 = learned_bucket_items_log2(ceil_log2(n));
+  t.bucket_log2        = std::clamp(ceil_log2(n) - items_log2, 8, LEARNED_MAX_BUCKET_LOG2);
+  t.bucket_cap         = 2 << items_log2;
   t.passes         = (t.bucket_log2 + RADIX_BITS - 1) / RADIX_BITS;
   t.tile_items     = persistent_tile_items(s.pass_tpb, s.pass_items);
   t.portion_items  = ((1ull << 30) - 1) / t.tile_items * t.tile_items; // 30-bit look-back counts
@@ -109,7 +111,7 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
   t.sample_temp_bytes = plan_radix_temp(s.sample_pol, LEARNED_SAMPLE, 0, 8 * kb, false, true).total_bytes;
   off += align_up(t.sample_temp_bytes, 256);
   t.bounds_off = off;
-  off += align_up(2 * 8 * (size_t(1) << t.bucket_log2), 256); // begins, ends
+  off += 256 + align_up(3 * 8 * (size_t(1) << t.bucket_log2), 256); // counters; begins, ends, rest_ends
   t.keys_tmp_off = off;
   if (!c.overwrite)
   {
@@ -176,6 +178,11 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
   {
     throw cuda_error(CUDA_ERROR_INVALID_VALUE, "key/value buffer is null");
   }
+  if (vb > 0 && !has_vals)
+  {
+    // the kernels of a pairs build move values unconditionally
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "the build sorts pairs but the values are null");
+  }
 
   auto* base          = static_cast<unsigned char*>(c.d_temp_storage);
   auto* ctrl          = reinterpret_cast<SortControl*>(base + t.ctrl_off);
@@ -185,8 +192,10 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
                          reinterpret_cast<uint32_t*>(base + t.lookback_off) + t.lookback_words};
   auto* model         = reinterpret_cast<LearnedModel*>(base + t.model_off);
   void* sample[2]     = {base + t.sample_off, base + t.sample_off + align_up(size_t(LEARNED_SAMPLE) * kb, 256)};
-  auto* begins        = reinterpret_cast<unsigned long long*>(base + t.bounds_off);
+  auto* bucket_ctrs   = reinterpret_cast<uint32_t*>(base + t.bounds_off);
+  auto* begins        = reinterpret_cast<unsigned long long*>(base + t.bounds_off + 256);
   auto* ends          = begins + (size_t(1) << t.bucket_log2);
+  auto* rest_ends     = ends + (size_t(1) << t.bucket_log2);
 
   void* keys_tmp      = base + t.keys_tmp_off;
   void* values_tmp    = base + t.values_tmp_off;
@@ -322,8 +331,8 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
   // 7. begin and end of every bucket, from one read of the partitioned keys
   {
     InitParams z{};
-    z.words     = reinterpret_cast<uint32_t*>(begins);
-    z.num_words = 4 * (uint64_t(1) << t.bucket_log2);
+    z.words     = bucket_ctrs; // the counters, begins and ends
+    z.num_words = 64 + 4 * (uint64_t(1) << t.bucket_log2);
     launch("learned_init", s.lk.init, unsigned(std::min<uint64_t>(ceil_div(z.num_words, 256), uint64_t(sms) * 8)),
            256, 0, c.stream, z);
     LearnedBoundsParams p{};
@@ -347,13 +356,34 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     {
       other_vals = part_vals == c.values[0] ? c.values[1] : part_vals == c.values[1] ? c.values[0] : c.values[1];
     }
+    // 8a. buckets of up to bucket_cap keys: one wide counting pass each, in shared memory
+    {
+      LearnedBucketParams bp{};
+      bp.keys_in     = part_keys;
+      bp.values_in   = part_vals;
+      bp.keys_out    = final_keys;
+      bp.values_out  = has_vals ? (final_keys == part_keys ? part_vals : other_vals) : nullptr;
+      bp.begins      = begins;
+      bp.ends        = ends;
+      bp.rest_ends   = rest_ends;
+      bp.counters    = bucket_ctrs;
+      bp.num_buckets = uint32_t(1u << t.bucket_log2);
+      bp.num_items   = n;
+      bp.codec       = codec;
+      const CUkernel k    = t.bucket_cap == 4096 ? s.lk.bucket4k : s.lk.bucket8k;
+      const int tpb       = learned_bucket_tpb(t.bucket_cap);
+      const size_t smem   = learned_bucket_smem(kb, vb, t.bucket_cap);
+      const unsigned grid = unsigned(sms * occupancy(k, tpb, smem));
+      launch("learned_bucket", k, grid, unsigned(tpb), smem, c.stream, bp);
+    }
+    // 8b. the rest (larger buckets, buckets with long runs of equal top bits): segmented radix sort
     SegmentedCall sc      = bucket_sort_call(s, c, t);
     sc.keys[0]            = part_keys;
     sc.keys[1]            = other_keys;
     sc.values[0]          = part_vals;
     sc.values[1]          = other_vals;
     sc.begin_offsets      = begins;
-    sc.end_offsets        = ends;
+    sc.end_offsets        = rest_ends;
     sc.target             = final_keys == part_keys ? 0 : 1;
     sc.d_temp_storage     = base + t.seg_off;
     size_t bytes          = t.seg_bytes;
@@ -402,7 +432,11 @@ LearnedStats learned_sort_stats(const LearnedSetup& s, const RadixCall& c)
   uint32_t w[SEG_CTR_WORDS];
   check(cuMemcpyDtoH(w, CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.seg_off), sizeof(w)),
         "cuMemcpyDtoH(learned stats)");
-  st.block_buckets  = w[SEG_CTR_SMALL] + w[SEG_CTR_MEDIUM] + w[SEG_CTR_BLOCK_S] + w[SEG_CTR_BLOCK_L];
+  uint32_t bucket_ctrs[2];
+  check(cuMemcpyDtoH(bucket_ctrs, CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.bounds_off),
+                     sizeof(bucket_ctrs)),
+        "cuMemcpyDtoH(learned stats)");
+  st.block_buckets = bucket_ctrs[1] + w[SEG_CTR_SMALL] + w[SEG_CTR_MEDIUM] + w[SEG_CTR_BLOCK_S] + w[SEG_CTR_BLOCK_L];
   st.device_buckets = w[SEG_CTR_DEVICE];
   std::memcpy(&st.device_items, &w[SEG_CTR_DEVICE_ITEMS], sizeof(st.device_items));
   return st;

@@ -1,6 +1,7 @@
 // Host dispatcher of the learned-partition sort: sample -> plain radix sort of the sample
 // -> least-squares fit -> digit counts -> stable partition passes on the bucket id -> bucket
-// bounds (one read of the partitioned keys) -> batched segmented sort of the buckets. Inputs it does not take (fewer
+// bounds (one read of the partitioned keys) -> bucket sort in shared memory (one wide counting pass per bucket) ->
+// batched segmented radix sort of the buckets that one could not take. Inputs it does not take (fewer
 // than LEARNED_MIN_ITEMS keys, a partial bit window, buffers that are not 16-byte aligned)
 // run the plain radix sort instead; the output and the selector are the plain sort's either way.
 #pragma once
@@ -25,6 +26,8 @@ struct LearnedKernels
   CUkernel hist;
   CUkernel pass;
   CUkernel bounds;
+  CUkernel bucket4k; // bucket sort, up to 4096 keys per bucket
+  CUkernel bucket8k; // up to 8192
 };
 
 // Everything one (key type, value width, order) needs; lives in the build result.
@@ -51,6 +54,7 @@ struct LearnedTempPlan
 {
   bool learned; // false: the plain radix sort runs (plain_bytes of temp)
   int bucket_log2;
+  int bucket_cap; // largest bucket the shared-memory bucket sort takes (twice the target size)
   int passes;
   uint64_t tile_items, portion_items, num_portions;
   size_t ctrl_off, ctrl_bytes, bins_off, lookback_off, lookback_words;

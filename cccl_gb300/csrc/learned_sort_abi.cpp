@@ -190,6 +190,9 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
     s->lk.hist   = get_kernel(r.learned_library, "gb300_learned_hist_k" + k + "_" + fs);
     s->lk.pass   = get_kernel(r.learned_library, "gb300_learned_pass_k" + k + "_v" + std::to_string(vb) + "_" + fs);
     s->lk.bounds = get_kernel(r.learned_library, "gb300_learned_bounds_k" + k + "_" + fs);
+    const std::string kvf = "_k" + k + "_v" + std::to_string(vb) + "_" + fs;
+    s->lk.bucket4k        = get_kernel(r.learned_library, "gb300_learned_bucket4096" + kvf);
+    s->lk.bucket8k        = get_kernel(r.learned_library, "gb300_learned_bucket8192" + kvf);
     *build = r;
     return CUDA_SUCCESS;
   }

@@ -116,6 +116,11 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
   const bool has_vals  = vb > 0 && c.values[0] != nullptr;
   const uint64_t n     = c.num_items;
   *selector            = 0;
+  if (c.d_temp_storage != nullptr && c.num_items > 0 && vb > 0 && c.values[0] == nullptr)
+  {
+    // the kernels of a pairs build move values unconditionally
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "the build sorts pairs but the values are null");
+  }
 
   if (c.begin_bit < 0 || c.end_bit > 8 * kb || c.begin_bit > c.end_bit)
   {

@@ -88,6 +88,11 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   const uint64_t n    = c.num_items;
   const uint64_t nseg = c.num_segments;
   *selector           = 0;
+  if (c.d_temp_storage != nullptr && c.num_items > 0 && vb > 0 && c.values[0] == nullptr)
+  {
+    // the kernels of a pairs build move values unconditionally
+    throw cuda_error(CUDA_ERROR_INVALID_VALUE, "the build sorts pairs but the values are null");
+  }
 
   // ---- digit passes of the large segments and the buffer that receives the result ----
   // DeviceSegmentedSort: CUB's large segments take ceil(key bits / 6) passes (4-bit digits

@@ -274,6 +274,23 @@ struct LearnedPassParams
   int digit_shift; // this pass's digit = (bucket >> digit_shift) & 255
 };
 
+// Bucket sort of the learned path: one wide counting pass per bucket in shared memory.
+struct LearnedBucketParams
+{
+  const void* keys_in; // partitioned (raw) keys
+  const void* values_in;
+  void* keys_out; // may alias keys_in: every bucket is read completely before it is written
+  void* values_out;
+  const unsigned long long* begins;
+  const unsigned long long* ends;
+  unsigned long long* rest_ends; // per bucket: ends[b] if the bucket is left to the segmented sort, else begins[b]
+  uint32_t* counters;            // [0] bucket ticket, [1] buckets sorted here (zeroed before the launch)
+  uint32_t num_buckets;
+  uint32_t pad0;
+  unsigned long long num_items;  // of the whole array (bounds the L2 prefetches)
+  KeyCodec codec;
+};
+
 struct LearnedBoundsParams
 {
   const void* keys; // partitioned (raw) keys: bucket ids are non-decreasing along them

@@ -333,8 +333,41 @@ GB300_HD constexpr size_t learned_pass_smem(int kb, int vb)
 constexpr int LEARNED_FIT_TPB    = LEARNED_SAMPLE / LEARNED_LEAVES; // one sample point per thread
 // Smallest input the learned path takes; below it the plain radix sort runs.
 constexpr unsigned long long LEARNED_MIN_ITEMS = 1ull << 20;
-// Target keys per bucket: ~4096, the block sort class (two partition passes up to 2^28 keys).
-// 64-key buckets of 8-byte keys (one more partition pass, radix-order merge networks of 8 x 8
-// and 32 x 8 keys) measured slower on GB300: f64 + i64 at 2^30, 102 ms against 81 ms.
-constexpr int LEARNED_BUCKET_ITEMS_LOG2 = 12;
+// Target keys per bucket: 2048 or 4096 (learned_bucket_items_log2). 64-key buckets of 8-byte
+// keys (one more partition pass, radix-order merge networks of 8 x 8 and 32 x 8 keys)
+// measured slower on GB300: f64 + i64 at 2^30, 102 ms against 81 ms.
+
+// Bucket sort of the learned path (one bucket per CTA at a time): buckets
+// of up to CAP keys are sorted by one counting pass on their top varying bits with as many
+// bins as keys, then every run of equal bins (at most LEARNED_RUN_MAX keys) is ordered by
+// comparison. Larger buckets and longer runs go to the segmented radix sort. CAP is twice
+// the target bucket size: 2048-key buckets (CAP 4096) unless that costs a partition pass,
+// else 4096-key buckets (CAP 8192).
+constexpr int LEARNED_RUN_MAX = 32;
+// 8 keys per thread: 512 threads for CAP 4096 (two CTAs per SM), 1024 for CAP 8192
+GB300_HD constexpr int learned_bucket_tpb(int cap)
+{
+  return cap / 8;
+}
+template <int KB, int VB, int CAP>
+struct LearnedBucketSmem
+{
+  static constexpr size_t kraw_off = 0;
+  static constexpr size_t vst_off  = round16(size_t(KB) * CAP);
+  static constexpr size_t bins_off = vst_off + round16(size_t(VB) * CAP);
+  static constexpr size_t perm_off = bins_off + size_t(4) * CAP;
+  static constexpr size_t bytes    = perm_off + size_t(2) * CAP;
+};
+GB300_HD constexpr size_t learned_bucket_smem(int kb, int vb, int cap)
+{
+  return round16(size_t(kb) * cap) + round16(size_t(vb) * cap) + size_t(4) * cap + size_t(2) * cap;
+}
+// log2 of the target bucket size for log2n = ceil(log2(num_items)): 2048-key buckets when
+// that needs no more partition passes than 4096-key buckets, else 4096.
+GB300_HD constexpr int learned_bucket_items_log2(int log2n)
+{
+  const int b11 = log2n - 11 < 8 ? 8 : (log2n - 11 > LEARNED_MAX_BUCKET_LOG2 ? LEARNED_MAX_BUCKET_LOG2 : log2n - 11);
+  const int b12 = log2n - 12 < 8 ? 8 : (log2n - 12 > LEARNED_MAX_BUCKET_LOG2 ? LEARNED_MAX_BUCKET_LOG2 : log2n - 12);
+  return (b11 + 7) / 8 == (b12 + 7) / 8 ? 11 : 12;
+}
 } // namespace gb300

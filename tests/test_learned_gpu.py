@@ -23,8 +23,11 @@ def _lib(built_library):
 
 
 def _expected_buckets(n, key_bytes):
-    """About 4096 keys per bucket, 2^8 to 2^24 buckets, whatever the key width."""
-    b = min(max(int(np.ceil(np.log2(n))) - 12, 8), 24)
+    """2048 keys per bucket where that takes no more partition passes than 4096, else 4096;
+    2^8 to 2^24 buckets, whatever the key width."""
+    log2n = int(np.ceil(np.log2(n)))
+    b11, b12 = (min(max(log2n - i, 8), 24) for i in (11, 12))
+    b = b11 if (b11 + 7) // 8 == (b12 + 7) // 8 else b12
     return b, (b + 7) // 8
 
 
@@ -135,12 +138,12 @@ def test_bit_window_takes_the_plain_path(oracle):
 
 
 def test_larger_bucket_count(oracle):
-    # 2^25 keys: 2^13 buckets, two passes; the bucket id's top digit has 5 bits
+    # 2^25 keys: 2^14 buckets of 2048 keys, two passes; the bucket id's top digit has 6 bits
     n = 1 << 25
     rng = np.random.default_rng(21)
     k = I.lognormal(np.float32, n, rng, 0.0, 2.0)
     st = _check(oracle, k, I.index_values(n))
-    assert st["bucket_log2"] == 13 and st["partition_passes"] == 2
+    assert (st["bucket_log2"], st["partition_passes"]) == _expected_buckets(n, 4) == (14, 2)
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=lambda d: np.dtype(d).name)
