@@ -347,9 +347,9 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
 // bucket id changes from a to b at index i, begins[b] = ends[a] = i, and the last key's bucket
 // ends at n. Empty buckets keep the zeros they were cleared to (begin == end). Warp w covers keys
 // [w * 32 * ITEMS, (w + 1) * 32 * ITEMS), lane l the keys l, l + 32, ...; the bucket of the
-// key before each comes from the neighbouring lane.
+// key before each comes from the neighbouring lane. A warp's keys are all loaded before the
+// first is used (ITEMS = learned_bounds_items: as many loads in flight as registers allow).
 // ---------------------------------------------------------------------------------------
-constexpr int LEARNED_BOUNDS_ITEMS = 16;
 
 template <int KB, int FP>
 __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p)
@@ -365,7 +365,8 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
   const U* keys                = static_cast<const U*>(p.keys);
   const int lane               = threadIdx.x & 31;
   const unsigned long long warps_total = (unsigned long long) gridDim.x * (blockDim.x >> 5);
-  const unsigned long long chunk       = 32ull * LEARNED_BOUNDS_ITEMS;
+  constexpr int ITEMS                  = learned_bounds_items(KB);
+  const unsigned long long chunk       = 32ull * ITEMS;
   auto bucket_at = [&](unsigned long long i) {
     return learned_bucket<U, FP>(encode_key<U>(keys[i], p.codec), tables, scale, bmax);
   };
@@ -373,14 +374,22 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
        w * chunk < n; w += warps_total)
   {
     const unsigned long long first = w * chunk;
+    // the chunk's keys are loaded before any is used, so their loads overlap
+    U k[ITEMS];
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it)
+    {
+      const unsigned long long i = first + (unsigned long long) it * 32 + lane;
+      k[it]                      = i < n ? __ldcs(keys + i) : U(0);
+    }
     // bucket of the key before this warp's chunk (none before index 0)
     long long carry = first == 0 ? -1ll : (long long) bucket_at(first - 1);
-#pragma unroll 1
-    for (int it = 0; it < LEARNED_BOUNDS_ITEMS; ++it)
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it)
     {
       const unsigned long long i = first + (unsigned long long) it * 32 + lane;
       const bool valid           = i < n;
-      const long long b          = valid ? (long long) bucket_at(i) : -2ll;
+      const long long b          = valid ? (long long) learned_bucket<U, FP>(encode_key<U>(k[it], p.codec), tables, scale, bmax) : -2ll;
       long long prev             = __shfl_up_sync(0xffffffffu, b, 1);
       if (lane == 0)
       {
@@ -412,12 +421,14 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
 // tie-break the plain sort uses. A bucket whose largest bin holds more than RUN_MAX keys
 // is left to the segmented radix sort (rest_ends[b] = ends[b]).
 //
-// Every thread keeps its PER keys and values in registers from load to the final placement
-// (all loads of a bucket precede all of its stores, so the output may alias the input);
-// shared memory holds the keys for the comparisons, the bins (start | count << 16 after
-// the scan) and, for bins of two or more keys, their members' indices. The sorted bucket
-// is assembled in shared memory and stored with coalesced writes: scattered 4- and 8-byte
-// stores cost one L1 transaction each and were the kernel's bottleneck.
+// Every thread keeps its PER keys in registers from load to the final placement, and the
+// values wait in shared memory in input order (all loads of a bucket precede all of its
+// stores, so the output may alias the input); shared memory also holds the ordering keys
+// for the comparisons, the bins (start | count << 16 after the scan) and, for bins of two
+// or more keys, their members' indices. The sorted keys are assembled in shared memory,
+// the values gathered through the input index of every sorted slot, and both stored with
+// coalesced writes: scattered 4- and 8-byte stores cost one L1 transaction each and were
+// the kernel's bottleneck.
 // ---------------------------------------------------------------------------------------
 template <int KB, int VB, int FP, int TPB, int CAP>
 __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p)
@@ -525,38 +536,42 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
     }
     const int s       = 32 - __clz(n - 1); // bins = 2^s >= n
     const uint32_t nb = 1u << s;
+    // Rows of slots that hold keys: slot j of every thread is empty for j >= rows. Buckets
+    // average half of CAP, so every per-slot loop below skips the empty rows (a CTA-uniform
+    // branch) instead of running them predicated off.
+    const int rows = int((n + TPB - 1) / TPB);
 
     // ---- load (registers and shared memory); clear the bins; range of the ordering keys ----
+    // keys in registers, values in shared memory in input order (vst[i])
     U kr[PER];
-    V vr[VB > 0 ? PER : 1];
 #pragma unroll
     for (int j = 0; j < PER; ++j)
     {
       const uint32_t i = tid + j * TPB;
-      kr[j]            = i < n ? kin[beg + i] : U(0);
-    }
-    if constexpr (VB > 0)
-    {
-#pragma unroll
-      for (int j = 0; j < PER; ++j)
+      if (j < rows && i < n)
       {
-        const uint32_t i = tid + j * TPB;
-        vr[j]            = i < n ? vin[beg + i] : V(0);
+        kr[j] = kin[beg + i];
+        if constexpr (VB > 0)
+        {
+          vst[i] = vin[beg + i];
+        }
       }
     }
     for (uint32_t i = tid; i < nb; i += TPB)
     {
       bins[i] = 0u;
     }
+    // kraw holds the ordering keys t until the comparisons are done, then the raw keys of
+    // the sorted bucket
     U lo = U(~U(0)), hi = U(0);
 #pragma unroll
     for (int j = 0; j < PER; ++j)
     {
       const uint32_t i = tid + j * TPB;
-      if (i < n)
+      if (j < rows && i < n)
       {
-        kraw[i]   = kr[j];
         const U t = key_of(kr[j]);
+        kraw[i]   = t;
         lo        = t < lo ? t : lo;
         hi        = t > hi ? t : hi;
       }
@@ -586,12 +601,12 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
       for (int j = 0; j < PER; ++j)
       {
         const uint32_t i = tid + j * TPB;
-        if (i < n)
+        if (j < rows && i < n)
         {
           kout[beg + i] = kr[j];
           if constexpr (VB > 0)
           {
-            vout[beg + i] = vr[j];
+            vout[beg + i] = vst[i]; // this thread's own slot
           }
         }
       }
@@ -605,9 +620,10 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
 #pragma unroll
       for (int j = 0; j < PER; ++j)
       {
-        sub[j] = uint32_t(U(key_of(kr[j]) - lo) >> shift);
-        if (tid + j * TPB < n)
+        const uint32_t i = tid + j * TPB;
+        if (j < rows && i < n)
         {
+          sub[j] = uint32_t(U(kraw[i] - lo) >> shift); // this thread's own slot
           atomicAdd(&bins[sub[j]], 1u);
         }
       }
@@ -682,7 +698,7 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
         {
           const uint32_t i = tid + j * TPB;
           pos[j]           = 0xffffffffu;
-          if (i < n)
+          if (j < rows && i < n)
           {
             const uint32_t w = bins[sub[j]];
             if ((w >> 16) == 1u)
@@ -701,7 +717,7 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
         for (int j = 0; j < PER; ++j)
         {
           const uint32_t i = tid + j * TPB;
-          if (i < n && pos[j] == 0xffffffffu)
+          if (j < rows && i < n && pos[j] == 0xffffffffu)
           {
             const uint32_t w  = bins[sub[j]];
             const uint32_t b1 = w & 0xffffu;
@@ -717,28 +733,30 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
             }
             else
             {
-              const U ti = key_of(kr[j]);
+              const U ti = kraw[i];
               for (uint32_t r = b0; r < b1; ++r)
               {
                 const uint32_t m = perm[r];
-                const U tm       = key_of(kraw[m]);
+                const U tm       = kraw[m];
                 rank += (tm < ti || (tm == ti && m < i)) ? 1u : 0u;
               }
             }
             pos[j] = b0 + rank;
           }
         }
-        __syncthreads(); // every comparison read of kraw is done
-        // sorted order in shared memory, then coalesced stores
+        __syncthreads(); // every comparison read of kraw and perm is done
+        // sorted keys in shared memory, and for every sorted slot the input index of its
+        // key (perm, free after the ranking), which gathers the values; coalesced stores
 #pragma unroll
         for (int j = 0; j < PER; ++j)
         {
-          if (tid + j * TPB < n)
+          const uint32_t i = tid + j * TPB;
+          if (j < rows && i < n)
           {
             kraw[pos[j]] = kr[j];
             if constexpr (VB > 0)
             {
-              vst[pos[j]] = vr[j];
+              perm[pos[j]] = uint16_t(i);
             }
           }
         }
@@ -747,12 +765,12 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
         for (int j = 0; j < PER; ++j)
         {
           const uint32_t q = tid + j * TPB;
-          if (q < n)
+          if (j < rows && q < n)
           {
             kout[beg + q] = kraw[q];
             if constexpr (VB > 0)
             {
-              vout[beg + q] = vst[q];
+              vout[beg + q] = vst[perm[q]];
             }
           }
         }

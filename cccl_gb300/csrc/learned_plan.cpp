@@ -343,7 +343,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     p.ends        = ends;
     p.codec       = codec;
     p.bucket_log2 = t.bucket_log2;
-    const uint64_t warps = ceil_div(n, 32ull * 16);
+    const uint64_t warps = ceil_div(n, 32ull * learned_bounds_items(kb));
     const unsigned grid  = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(warps, 8), uint64_t(sms) * 16)));
     launch("learned_bounds", s.lk.bounds, grid, 256, 0, c.stream, p);
   }

@@ -331,6 +331,13 @@ GB300_HD constexpr size_t learned_pass_smem(int kb, int vb)
 }
 
 constexpr int LEARNED_FIT_TPB    = LEARNED_SAMPLE / LEARNED_LEAVES; // one sample point per thread
+// Keys per lane of the bucket-bounds kernel, all loaded before the first is used: 16 for
+// 4-byte keys; 8 for 8-byte keys, whose 16 took 82 registers and a quarter of the warps
+// (f64 at 2^30: 4.7 against 4.0 ms with one key per lane at a time).
+GB300_HD constexpr int learned_bounds_items(int kb)
+{
+  return kb == 8 ? 8 : 16;
+}
 // Smallest input the learned path takes; below it the plain radix sort runs.
 constexpr unsigned long long LEARNED_MIN_ITEMS = 1ull << 20;
 // Target keys per bucket: 2048 or 4096 (learned_bucket_items_log2). 64-key buckets of 8-byte
