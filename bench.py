@@ -8,6 +8,10 @@ between steps. Reported beside the headline line:
   * "variants": the same configuration at AND-reduced entropies, a constant key,
     descending, begin_bit 8 / end_bit 40; 2^28 uint32 keys-only (the roofline row) and
     2^24 uint32 keys-only with L2 flushed between steps;
+  * "e2e": the same sort with its inputs uploaded from pinned host memory and its result
+    read back every step, over back-to-back batches: two device buffer sets and three
+    streams, so batch i+1 uploads and batch i-1 downloads while batch i sorts (the host
+    link carries both directions at once); the one-batch-at-a-time step is reported beside it;
   * "segmented": the batched segmented sort of 2^27 f32 keys + i32 values in lognormal
     segments, plain and CUDA-graph replay, against one plain sort launch per segment;
   * "learned": the learned-partition sort against the plain sort on 2^28 f32 + u32
@@ -572,19 +576,24 @@ def run_engine(args):
     if tf.exists():
         traffic = json.loads(tf.read_text()).get("pairs_u64_u32_bytes_per_launch_at_2p28")
 
-    # end to end: pinned host buffers -> device -> sort -> host, through the same C ABI
+    # End to end through the same C ABI: every step uploads its batch (keys and values) from
+    # pinned host memory and reads its sorted result back into pinned host memory.
+    #   single:    one step at a time (upload, sort, download);
+    #   pipelined: back-to-back batches on two device buffer sets and three streams, so the
+    #              upload of batch i+1 and the download of batch i-1 run beside the sort of
+    #              batch i (the host link carries both directions at once).
     hk = torch.empty(n, dtype=torch.int64, pin_memory=True)
     hv = torch.empty(n, dtype=torch.int32, pin_memory=True)
     hk.copy_(keys.view(torch.int64))
     hv.copy_(main.vi)
-    ok = torch.empty_like(hk, pin_memory=True)
-    ov = torch.empty_like(hv, pin_memory=True)
+    outs = [(torch.empty_like(hk, pin_memory=True), torch.empty_like(hv, pin_memory=True)) for _ in range(2)]
 
-    # keys and values cross the host link on two streams at once (separate copy engines)
+    # single: keys and values cross the host link on two streams at once (separate copy engines)
     cur = torch.cuda.current_stream()
     side = [torch.cuda.Stream(), torch.cuda.Stream()]
 
     def e2e_step():
+        ok, ov = outs[0]
         for st in side:
             st.wait_stream(cur)
         with torch.cuda.stream(side[0]):
@@ -604,8 +613,54 @@ def run_engine(args):
             cur.wait_stream(st)
 
     e2e_steps = max(3, args.steps // 2)
-    e2e_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
+    e2e_single_ms = time_steps(torch, e2e_step, e2e_steps, 1, barrier)
     torch.cuda.synchronize()
+
+    # pipelined
+    sets = [main, Sorter(torch, torch.empty_like(keys), with_values=True)]
+    up, comp, down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    uploaded = [torch.cuda.Event() for _ in sets]
+    sorted_ev = [torch.cuda.Event() for _ in sets]
+    downloaded = [torch.cuda.Event() for _ in sets]
+    used = [False, False]
+
+    def pipelined(steps):
+        for i in range(steps):
+            b = i % 2
+            s = sets[b]
+            if used[b]:
+                up.wait_event(downloaded[b])  # the set's previous result has been read back
+            with torch.cuda.stream(up):
+                s.ki.view(torch.int64).copy_(hk, non_blocking=True)
+                s.vi.copy_(hv, non_blocking=True)
+                uploaded[b].record(up)
+            comp.wait_event(uploaded[b])
+            s.run(stream=comp)
+            sorted_ev[b].record(comp)
+            down.wait_event(sorted_ev[b])
+            with torch.cuda.stream(down):
+                outs[b][0].copy_(s.ko.view(torch.int64), non_blocking=True)
+                outs[b][1].copy_(s.vo, non_blocking=True)
+                downloaded[b].record(down)
+            used[b] = True
+
+    pipelined(max(3, args.warmup))
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(up)
+    pipelined(e2e_steps)
+    t1.record(down)
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / e2e_steps
+    last = (e2e_steps + max(3, args.warmup) - 1) % 2
+    e2e_ok = bool(torch.equal(outs[last][0], sets[last].ko.view(torch.int64).cpu())
+                  and torch.equal(outs[last][1], sets[last].vo.cpu()))
+    del sets
+    torch.cuda.empty_cache()
 
     # the batched segmented configuration and the learned-partition workloads
     segmented = None
@@ -694,7 +749,12 @@ def run_engine(args):
         "gpu_launches": launches * args.steps,
         "clocks": clocks.summary(),
         "e2e": {"value": n / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 12,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms,
+                "mode": "pipelined: back-to-back batches, two device buffer sets, the upload of batch i+1 "
+                        "and the download of batch i-1 beside the sort of batch i",
+                "downloaded_result_matches_device": e2e_ok,
+                "single_step": {"value": n / (e2e_single_ms / 1000.0), "ms_per_step": e2e_single_ms,
+                                "mode": "one batch at a time: upload, sort, download"}},
         "cpu_baseline": cpu,
         "variants": variants,
         "segmented": segmented,
