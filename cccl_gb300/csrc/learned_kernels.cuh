@@ -30,7 +30,9 @@ struct alignas(16) LearnedLeaf
   float icpt;
 };
 
-// Shared-memory copy of the model (layout size: learned_tables_bytes()).
+// Shared-memory copy of the model for one sort (layout size: learned_tables_bytes()). Each
+// leaf's line is stored in buckets rather than sample ranks: slope and intercept times
+// scale = buckets / sample keys, a power of two, so the product is exact.
 template <class U>
 struct LearnedTables
 {
@@ -40,14 +42,21 @@ struct LearnedTables
   int shift;
 };
 
-template <class U>
-__device__ __forceinline__ void learned_load_tables(const LearnedModel* m, LearnedTables<U>* t)
+// 2^bucket_log2 buckets per 2^LEARNED_SAMPLE_LOG2 sample ranks
+__device__ __forceinline__ float learned_scale(int bucket_log2)
 {
+  return exp2f(float(bucket_log2 - LEARNED_SAMPLE_LOG2)); // a power of two: exact
+}
+
+template <class U>
+__device__ __forceinline__ void learned_load_tables(const LearnedModel* m, LearnedTables<U>* t, int bucket_log2)
+{
+  const float scale = learned_scale(bucket_log2);
   for (int i = threadIdx.x; i < LEARNED_LEAVES; i += blockDim.x)
   {
     t->leaf[i].knot  = U(m->knot[i]);
-    t->leaf[i].slope = m->slope[i];
-    t->leaf[i].icpt  = m->icpt[i];
+    t->leaf[i].slope = m->slope[i] * scale;
+    t->leaf[i].icpt  = m->icpt[i] * scale;
   }
   const uint32_t* src = reinterpret_cast<const uint32_t*>(m->cell_leaf);
   uint32_t* dst       = reinterpret_cast<uint32_t*>(t->cell_leaf);
@@ -98,30 +107,33 @@ __device__ __forceinline__ int learned_leaf(U k, const LearnedTables<U>& t)
   return j;
 }
 
-// Bucket of an encoded key. Every step is non-decreasing in the key: the leaf lookup, the
-// conversion of (key - knot) to float, the fused multiply-add with a slope >= 0, the clamp
-// to the leaf's rank range (leaf j's top equals leaf j+1's bottom) and the truncation after
-// scaling by a power of two.
+// Bucket of an encoded key: floor(clamp(rank, j * P, (j + 1) * P) * scale) for the predicted
+// sample rank of leaf j (P = sample keys per leaf). The tables hold the line times scale, a
+// power of two, so fmaf gives rank * scale exactly; the leaf's bucket range
+// [j * P * scale, (j + 1) * P * scale] is integral (at least 256 buckets), so the clamp is
+// applied after the truncation, in integers, with the same result. Every step is
+// non-decreasing in the key: the leaf lookup, the conversion of (key - knot) to float, the
+// fused multiply-add with a slope >= 0, the truncation (negative ranks give 0) and the
+// clamp to the leaf's range (leaf j's top equals leaf j+1's bottom).
 template <class U, int FP>
-__device__ __forceinline__ uint32_t
-learned_bucket(U enc, const LearnedTables<U>& t, float scale, uint32_t bmax)
+__device__ __forceinline__ uint32_t learned_bucket(U enc, const LearnedTables<U>& t, int range_log2, uint32_t bmax)
 {
-  const U k                = digit_source<U, FP>(enc);
-  const int j              = learned_leaf<U>(k, t);
-  const LearnedLeaf<U> lf  = t.leaf[j];
-  const float x            = k > lf.knot ? learned_to_float(U(k - lf.knot)) : 0.0f;
-  constexpr float span     = float(LEARNED_SAMPLE / LEARNED_LEAVES);
-  const float lo           = float(j) * span;
-  float r                  = fmaf(lf.slope, x, lf.icpt);
-  r                        = fminf(fmaxf(r, lo), lo + span);
-  const uint32_t b         = uint32_t(r * scale);
+  const U k               = digit_source<U, FP>(enc);
+  const int j             = learned_leaf<U>(k, t);
+  const LearnedLeaf<U> lf = t.leaf[j];
+  const float x           = k > lf.knot ? learned_to_float(U(k - lf.knot)) : 0.0f;
+  const uint32_t lo       = uint32_t(j) << range_log2;
+  uint32_t b              = __float2uint_rz(fmaf(lf.slope, x, lf.icpt));
+  b                       = min(max(b, lo), lo + (1u << range_log2));
   return b < bmax ? b : bmax;
 }
 
-__device__ __forceinline__ float learned_scale(int bucket_log2)
+// log2 of the buckets in one leaf's rank range: (sample / leaves) * scale
+__host__ __device__ constexpr int learned_range_log2(int bucket_log2)
 {
-  return exp2f(float(bucket_log2 - LEARNED_SAMPLE_LOG2)); // a power of two: exact
+  return bucket_log2 - (LEARNED_SAMPLE_LOG2 - 8);
 }
+static_assert(LEARNED_SAMPLE / LEARNED_LEAVES == 256, "leaf rank range of 2^8 sample keys");
 
 // ---------------------------------------------------------------------------------------
 // sample: thread i takes one key from [i*n/S, (i+1)*n/S) at a hashed offset
@@ -273,14 +285,14 @@ __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
   {
     sh[i] = 0;
   }
-  learned_load_tables<U>(p.model, &tables);
+  learned_load_tables<U>(p.model, &tables, p.bucket_log2);
   __syncthreads();
 
-  const float scale    = learned_scale(p.bucket_log2);
+  const int range_log2 = learned_range_log2(p.bucket_log2);
   const uint32_t bmax  = (1u << p.bucket_log2) - 1u;
   const int passes     = p.h.num_passes;
   auto count_key       = [&](U raw) {
-    const uint32_t b = learned_bucket<U, FP>(encode_key<U>(raw, p.h.codec), tables, scale, bmax);
+    const uint32_t b = learned_bucket<U, FP>(encode_key<U>(raw, p.h.codec), tables, range_log2, bmax);
 #pragma unroll
     for (int q = 0; q < MAX_PASSES; ++q)
     {
@@ -301,7 +313,7 @@ template <class U, int FP>
 struct LearnedPassHook
 {
   const LearnedModel* model;
-  float scale;
+  int bucket_log2;
   uint32_t bmax;
   int shift;
 
@@ -313,20 +325,21 @@ struct LearnedPassHook
 
   __device__ __forceinline__ void setup(unsigned char* extra) const
   {
-    learned_load_tables<U>(model, reinterpret_cast<LearnedTables<U>*>(extra));
+    learned_load_tables<U>(model, reinterpret_cast<LearnedTables<U>*>(extra), bucket_log2);
   }
 
   template <class K, int ITEMS>
   __device__ __forceinline__ void
   compute(const K (&keys)[ITEMS], uint32_t valid, int wofs, ComputedDigits<ITEMS>& dg, unsigned char* extra) const
   {
-    const auto& t = *reinterpret_cast<const LearnedTables<U>*>(extra);
-    dg.stage      = extra + tables_bytes;
+    const auto& t        = *reinterpret_cast<const LearnedTables<U>*>(extra);
+    const int range_log2 = learned_range_log2(bucket_log2);
+    dg.stage             = extra + tables_bytes;
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i)
     {
       const uint32_t idx = uint32_t(wofs + i * 32);
-      dg.d[i] = idx < valid ? (learned_bucket<U, FP>(keys[i], t, scale, bmax) >> shift) & 255u : 255u;
+      dg.d[i] = idx < valid ? (learned_bucket<U, FP>(keys[i], t, range_log2, bmax) >> shift) & 255u : 255u;
     }
   }
 };
@@ -338,7 +351,7 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
   constexpr int TPB   = persistent_tpb(KB, VB);
   constexpr int ITEMS = learned_items(KB, VB);
   constexpr size_t EXTRA = learned_extra_bytes(KB, VB, ITEMS);
-  const LearnedPassHook<U, FP> hook{p.model, learned_scale(p.bucket_log2), (1u << p.bucket_log2) - 1u, p.digit_shift};
+  const LearnedPassHook<U, FP> hook{p.model, p.bucket_log2, (1u << p.bucket_log2) - 1u, p.digit_shift};
   onesweep_persistent_body<KB, VB, FP, TPB, ITEMS, true, LearnedPassHook<U, FP>, EXTRA>(p.os, hook);
 }
 
@@ -356,11 +369,11 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
 {
   using U = typename uint_of<KB>::type;
   __shared__ LearnedTables<U> tables;
-  learned_load_tables<U>(p.model, &tables);
+  learned_load_tables<U>(p.model, &tables, p.bucket_log2);
   __syncthreads();
 
   const unsigned long long n   = p.num_items;
-  const float scale            = learned_scale(p.bucket_log2);
+  const int range_log2         = learned_range_log2(p.bucket_log2);
   const uint32_t bmax          = (1u << p.bucket_log2) - 1;
   const U* keys                = static_cast<const U*>(p.keys);
   const int lane               = threadIdx.x & 31;
@@ -368,7 +381,7 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
   constexpr int ITEMS                  = learned_bounds_items(KB);
   const unsigned long long chunk       = 32ull * ITEMS;
   auto bucket_at = [&](unsigned long long i) {
-    return learned_bucket<U, FP>(encode_key<U>(keys[i], p.codec), tables, scale, bmax);
+    return learned_bucket<U, FP>(encode_key<U>(keys[i], p.codec), tables, range_log2, bmax);
   };
   for (unsigned long long w = blockIdx.x * (unsigned long long) (blockDim.x >> 5) + (threadIdx.x >> 5);
        w * chunk < n; w += warps_total)
@@ -389,7 +402,7 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
     {
       const unsigned long long i = first + (unsigned long long) it * 32 + lane;
       const bool valid           = i < n;
-      const long long b          = valid ? (long long) learned_bucket<U, FP>(encode_key<U>(k[it], p.codec), tables, scale, bmax) : -2ll;
+      const long long b          = valid ? (long long) learned_bucket<U, FP>(encode_key<U>(k[it], p.codec), tables, range_log2, bmax) : -2ll;
       long long prev             = __shfl_up_sync(0xffffffffu, b, 1);
       if (lane == 0)
       {

@@ -313,9 +313,17 @@ GB300_HD constexpr size_t learned_extra_bytes(int kb, int vb, int items)
   return (void) kb, learned_tables_bytes() + round16(size_t(persistent_main(kb, vb)) * items);
 }
 
+// Items per main thread of the partition pass before the shared-memory fit: the pass holds
+// the computed digits in registers beside the keys, values and positions, so 4-byte keys with
+// 4-byte values take 10 (12, the shared-memory bound, spilled 84 bytes per thread).
+GB300_HD constexpr int learned_items_nominal(int kb, int vb)
+{
+  return kb == 4 && vb == 4 && persistent_items_nominal(kb, vb) > 10 ? 10 : persistent_items_nominal(kb, vb);
+}
+
 GB300_HD constexpr int learned_items(int kb, int vb)
 {
-  int items = persistent_items_nominal(kb, vb);
+  int items = learned_items_nominal(kb, vb);
   while (items > 1
          && (persistent_smem_for(kb, vb, items) + learned_extra_bytes(kb, vb, items)) * PERSISTENT_MINB
               > size_t(227) * 1024)
