@@ -9,7 +9,7 @@ between steps. Reported beside the headline line:
     descending, begin_bit 8 / end_bit 40; 2^28 uint32 keys-only (the roofline row) and
     2^24 uint32 keys-only with L2 flushed between steps;
   * "e2e": the same sort with its inputs uploaded from pinned host memory and its result
-    read back every step, over back-to-back batches: two device buffer sets and three
+    read back every step, over back-to-back batches: three device buffer sets and three
     streams, so batch i+1 uploads and batch i-1 downloads while batch i sorts (the host
     link carries both directions at once); the one-batch-at-a-time step is reported beside it;
   * "segmented": the batched segmented sort of 2^27 f32 keys + i32 values in lognormal
@@ -579,14 +579,17 @@ def run_engine(args):
     # End to end through the same C ABI: every step uploads its batch (keys and values) from
     # pinned host memory and reads its sorted result back into pinned host memory.
     #   single:    one step at a time (upload, sort, download);
-    #   pipelined: back-to-back batches on two device buffer sets and three streams, so the
+    #   pipelined: back-to-back batches on SETS device buffer sets and three streams, so the
     #              upload of batch i+1 and the download of batch i-1 run beside the sort of
-    #              batch i (the host link carries both directions at once).
+    #              batch i (the host link carries both directions at once). A set is busy
+    #              for its batch's upload, sort and download in turn, so three sets keep
+    #              every stream fed (two left the upload waiting for a download).
     hk = torch.empty(n, dtype=torch.int64, pin_memory=True)
     hv = torch.empty(n, dtype=torch.int32, pin_memory=True)
     hk.copy_(keys.view(torch.int64))
     hv.copy_(main.vi)
-    outs = [(torch.empty_like(hk, pin_memory=True), torch.empty_like(hv, pin_memory=True)) for _ in range(2)]
+    SETS = 3
+    outs = [(torch.empty_like(hk, pin_memory=True), torch.empty_like(hv, pin_memory=True)) for _ in range(SETS)]
 
     # single: keys and values cross the host link on two streams at once (separate copy engines)
     cur = torch.cuda.current_stream()
@@ -617,16 +620,16 @@ def run_engine(args):
     torch.cuda.synchronize()
 
     # pipelined
-    sets = [main, Sorter(torch, torch.empty_like(keys), with_values=True)]
+    sets = [main] + [Sorter(torch, torch.empty_like(keys), with_values=True) for _ in range(SETS - 1)]
     up, comp, down = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
     uploaded = [torch.cuda.Event() for _ in sets]
     sorted_ev = [torch.cuda.Event() for _ in sets]
     downloaded = [torch.cuda.Event() for _ in sets]
-    used = [False, False]
+    used = [False] * SETS
 
     def pipelined(steps):
         for i in range(steps):
-            b = i % 2
+            b = i % SETS
             s = sets[b]
             if used[b]:
                 up.wait_event(downloaded[b])  # the set's previous result has been read back
@@ -656,7 +659,7 @@ def run_engine(args):
     barrier()
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / e2e_steps
-    last = (e2e_steps + max(3, args.warmup) - 1) % 2
+    last = (e2e_steps + max(3, args.warmup) - 1) % SETS
     e2e_ok = bool(torch.equal(outs[last][0], sets[last].ko.view(torch.int64).cpu())
                   and torch.equal(outs[last][1], sets[last].vo.cpu()))
     del sets
@@ -750,7 +753,7 @@ def run_engine(args):
         "clocks": clocks.summary(),
         "e2e": {"value": n / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 12,
                 "ms_per_step": e2e_ms,
-                "mode": "pipelined: back-to-back batches, two device buffer sets, the upload of batch i+1 "
+                "mode": "pipelined: back-to-back batches, three device buffer sets, the upload of batch i+1 "
                         "and the download of batch i-1 beside the sort of batch i",
                 "downloaded_result_matches_device": e2e_ok,
                 "single_step": {"value": n / (e2e_single_ms / 1000.0), "ms_per_step": e2e_single_ms,
