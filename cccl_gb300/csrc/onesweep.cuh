@@ -69,6 +69,80 @@ struct ComputedDigits
   uint8_t* stage; // [TILE] digit of every staging slot
 };
 
+// Buffers and encode/decode flags a pass runs with: the launch's, or the ones its pass plan
+// gives (see PLAN_* in sort_params.h).
+struct PassIO
+{
+  const void* keys_in; // portion-relative
+  void* keys_out;
+  const void* values_in;
+  void* values_out;
+  int encode_in;
+  int decode_out;
+};
+
+// Resolves the pass's buffers. Returns false when the pass does nothing: gated off, or
+// skipped by its plan (its digit is the same for every key), in which case the grid first
+// clears this portion's rows of the next pass's look-back buffer, as the pass would have.
+template <int KB, int VB>
+__device__ __forceinline__ bool resolve_pass(const OnesweepParams& p, PassIO& io)
+{
+  if (!gate_open(p.gate))
+  {
+    return false;
+  }
+  io = PassIO{p.keys_in, p.keys_out, p.values_in, p.values_out, p.encode_in, p.decode_out};
+  if (p.plan == nullptr)
+  {
+    return true;
+  }
+  const uint32_t w = __ldcg(p.plan);
+  if (w & PLAN_SKIP)
+  {
+    if (p.lookback_next != nullptr)
+    {
+      uint32_t* rows                    = p.lookback_next + (size_t) p.tile_row_base * RADIX_DIGITS;
+      const unsigned long long words    = (unsigned long long) p.portion_tiles * RADIX_DIGITS;
+      const unsigned long long nthreads = (unsigned long long) gridDim.x * blockDim.x;
+      for (unsigned long long i = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; i < words; i += nthreads)
+      {
+        rows[i] = 0u;
+      }
+    }
+    return false;
+  }
+  const int si = int(w >> PLAN_SRC_SHIFT) & 3;
+  const int di = int(w >> PLAN_DST_SHIFT) & 3;
+  io.keys_in   = static_cast<const unsigned char*>(p.key_bufs[si]) + p.portion_begin * KB;
+  io.keys_out  = const_cast<void*>(p.key_bufs[di]);
+  if constexpr (VB > 0)
+  {
+    io.values_in  = static_cast<const unsigned char*>(p.value_bufs[si]) + p.portion_begin * VB;
+    io.values_out = const_cast<void*>(p.value_bufs[di]);
+  }
+  io.encode_in  = (w & PLAN_ENCODE) != 0u;
+  io.decode_out = (w & PLAN_DECODE) != 0u;
+  return true;
+}
+
+// The same for a kernel that passes its own copy q of the parameters to the pass body.
+template <int KB, int VB>
+__device__ __forceinline__ bool apply_pass_plan(OnesweepParams& q)
+{
+  PassIO io;
+  if (!resolve_pass<KB, VB>(q, io))
+  {
+    return false;
+  }
+  q.keys_in    = io.keys_in;
+  q.keys_out   = io.keys_out;
+  q.values_in  = io.values_in;
+  q.values_out = io.values_out;
+  q.encode_in  = io.encode_in;
+  q.decode_out = io.decode_out;
+  return true;
+}
+
 // Decoupled look-back of digit d for `tile` (tile > 0): the sum of the predecessors'
 // counts back to the nearest inclusive prefix. BATCH predecessor rows are read per step (one
 // L2 round trip): inclusive prefixes spread from tile to tile at about BATCH tiles per round
@@ -337,10 +411,15 @@ __device__ __forceinline__ void onesweep_tile(
 // first pass; padding keys of a partial tile are all-ones so they rank last.
 template <int KB, int TPB, int ITEMS>
 __device__ __forceinline__ void load_tile_keys_global(
-  const OnesweepParams& p, uint32_t tile_first, uint32_t valid, typename uint_of<KB>::type (&keys)[ITEMS])
+  const OnesweepParams& p,
+  const void* keys_in,
+  int encode_in,
+  uint32_t tile_first,
+  uint32_t valid,
+  typename uint_of<KB>::type (&keys)[ITEMS])
 {
   using U        = typename uint_of<KB>::type;
-  const U* kin   = static_cast<const U*>(p.keys_in) + tile_first;
+  const U* kin   = static_cast<const U*>(keys_in) + tile_first;
   const int wofs = (threadIdx.x >> 5) * ITEMS * 32 + (threadIdx.x & 31);
   if (valid == uint32_t(TPB * ITEMS))
   {
@@ -359,7 +438,7 @@ __device__ __forceinline__ void load_tile_keys_global(
       keys[i]            = idx < valid ? kin[idx] : U(~U(0));
     }
   }
-  if (p.encode_in)
+  if (encode_in)
   {
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i)
@@ -375,10 +454,10 @@ __device__ __forceinline__ void load_tile_keys_global(
 
 template <int VB, int TPB, int ITEMS>
 __device__ __forceinline__ void load_tile_values_global(
-  const OnesweepParams& p, uint32_t tile_first, uint32_t valid, typename value_word<VB>::type (&vals)[ITEMS])
+  const void* values_in, uint32_t tile_first, uint32_t valid, typename value_word<VB>::type (&vals)[ITEMS])
 {
   using V        = typename value_word<VB>::type;
-  const V* vin   = static_cast<const V*>(p.values_in) + tile_first;
+  const V* vin   = static_cast<const V*>(values_in) + tile_first;
   const int wofs = (threadIdx.x >> 5) * ITEMS * 32 + (threadIdx.x & 31);
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i)
@@ -430,11 +509,11 @@ __device__ __forceinline__ void onesweep_body(const OnesweepParams& p)
   const uint32_t tile_first = tile * L::TILE;
   const uint32_t valid      = min(uint32_t(L::TILE), p.portion_items - tile_first);
   U keys[ITEMS];
-  load_tile_keys_global<KB, TPB, ITEMS>(p, tile_first, valid, keys);
+  load_tile_keys_global<KB, TPB, ITEMS>(p, p.keys_in, p.encode_in, tile_first, valid, keys);
   onesweep_tile<KB, VB, FP, TPB, ITEMS, STABLE>(p, tile, valid, keys, whist, gdelta, misc, kstage, vstage, [&](auto& vals) {
     if constexpr (VB > 0)
     {
-      load_tile_values_global<VB, TPB, ITEMS>(p, tile_first, valid, vals);
+      load_tile_values_global<VB, TPB, ITEMS>(p.values_in, tile_first, valid, vals);
     }
   });
 }
@@ -482,7 +561,7 @@ struct PersistentSmem
 };
 // misc words: [2] sticky failure of the CTA (its stores are disabled), [3] single-digit
 // flag and digit of the tile being ranked, [4] digit of the tile's first key, [8..15] scan
-// scratch, [16..21] three mbarriers.
+// scratch, [16..21] three mbarriers, [22..31] the pass's buffers and flags (PassIO).
 
 // Pass hook of the persistent kernel: the plain radix pass has none. A hook may fill its
 // shared-memory region once per CTA (setup) and supply computed digits per tile.
@@ -496,8 +575,10 @@ struct PlainPassHook
   {}
 };
 
-template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE, class Hook = PlainPassHook, size_t EXTRA = 0>
-__device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p, const Hook& hook = Hook{})
+// FROM_PLAN: the pass's buffers and flags come from the resolved plan (res, kept in the misc
+// block) instead of the launch parameters.
+template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE, class Hook, size_t EXTRA, bool FROM_PLAN>
+__device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p, const Hook& hook, const PassIO& res)
 {
   using L            = PersistentSmem<KB, VB, TPB, ITEMS, EXTRA>;
   using U            = typename L::U;
@@ -515,6 +596,29 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
   long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
   uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);
   uint64_t* mbar    = reinterpret_cast<uint64_t*>(misc + 16);
+  PassIO* io        = reinterpret_cast<PassIO*>(misc + 22); // read where used: no registers held
+  static_assert(sizeof(PassIO) <= 10 * sizeof(uint32_t), "PassIO fits misc[22..31]");
+  // the pass's buffers and flags: launch parameters, or the plan's from shared memory
+  auto keys_in_of = [&]() -> const void* {
+    if constexpr (FROM_PLAN)
+    {
+      return io->keys_in;
+    }
+    else
+    {
+      return p.keys_in;
+    }
+  };
+  auto values_in_of = [&]() -> const void* {
+    if constexpr (FROM_PLAN)
+    {
+      return io->values_in;
+    }
+    else
+    {
+      return p.values_in;
+    }
+  };
   auto kbuf         = [&](int b) {
     return reinterpret_cast<U*>(smem + L::buf_off + size_t(b) * L::buf_bytes);
   };
@@ -522,10 +626,6 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
     return reinterpret_cast<V*>(smem + L::buf_off + size_t(b) * L::buf_bytes + L::kbytes);
   };
 
-  if (!gate_open(p.gate))
-  {
-    return;
-  }
   const int tid         = threadIdx.x;
   const uint32_t ntiles = p.portion_tiles;
   const int bit         = p.current_bit;
@@ -534,15 +634,16 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
   const uint32_t nfull = p.portion_items / TILE;
   auto issue           = [&](uint32_t t, int b) {
     mbar_arrive_expect_tx(&mbar[b], uint32_t(TILE * KB + (VB > 0 ? TILE * VB : 0)));
-    bulk_copy_g2s(kbuf(b), static_cast<const U*>(p.keys_in) + (size_t) t * TILE, uint32_t(TILE * KB), &mbar[b]);
+    bulk_copy_g2s(kbuf(b), static_cast<const U*>(keys_in_of()) + (size_t) t * TILE, uint32_t(TILE * KB), &mbar[b]);
     if constexpr (VB > 0)
     {
-      bulk_copy_g2s(vbuf(b), static_cast<const V*>(p.values_in) + (size_t) t * TILE, uint32_t(TILE * VB), &mbar[b]);
+      bulk_copy_g2s(vbuf(b), static_cast<const V*>(values_in_of()) + (size_t) t * TILE, uint32_t(TILE * VB), &mbar[b]);
     }
   };
 
   if (tid == 0)
   {
+    *io = res;
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
     mbar_init(&mbar[2], 1);
@@ -566,8 +667,8 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
     const int warp  = tid >> 5;
     const int lane  = tid & 31;
     const int wofs  = warp * ITEMS * 32 + lane;
-    U* kout         = static_cast<U*>(p.keys_out);
-    V* vout         = static_cast<V*>(p.values_out);
+    U* kout         = static_cast<U*>(FROM_PLAN ? io->keys_out : p.keys_out);
+    V* vout         = static_cast<V*>(FROM_PLAN ? io->values_out : p.values_out);
     uint8_t* dstage = nullptr; // computed digits of the staged tile
 
     // Consecutive staging slots of one digit go to consecutive outputs. Every store is
@@ -577,6 +678,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
       const U* ks                        = kbuf(b);
       const V* vs                        = vbuf(b);
       const bool full                    = valid == uint32_t(TILE);
+      const bool decode                  = (FROM_PLAN ? io->decode_out : p.decode_out) != 0;
       const unsigned long long out_limit = misc[2] != 0u ? 0ull : p.num_items_total;
 #pragma unroll
       for (int j = 0; j < ITEMS; ++j)
@@ -597,7 +699,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
           const long long g = gdelta[d] + (long long) s;
           if ((unsigned long long) g < out_limit)
           {
-            __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
+            __stcs(kout + g, decode ? decode_key<U>(k, p.codec) : k);
             if constexpr (VB > 0)
             {
               __stcs(vout + g, vs[s]);
@@ -643,7 +745,7 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
         {
           keys[i] = ks[wofs + i * 32];
         }
-        if (p.encode_in)
+        if (FROM_PLAN ? io->encode_in : p.encode_in)
         {
 #pragma unroll
           for (int i = 0; i < ITEMS; ++i)
@@ -663,10 +765,11 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
       }
       else
       {
-        load_tile_keys_global<KB, MT, ITEMS>(p, tile_first, valid, keys);
+        load_tile_keys_global<KB, MT, ITEMS>(p, keys_in_of(), FROM_PLAN ? io->encode_in : p.encode_in, tile_first,
+                                             valid, keys);
         if constexpr (VB > 0)
         {
-          load_tile_values_global<VB, MT, ITEMS>(p, tile_first, valid, vals);
+          load_tile_values_global<VB, MT, ITEMS>(values_in_of(), tile_first, valid, vals);
         }
       }
       Digits dg;
@@ -818,6 +921,36 @@ __device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p
       }
       asm volatile("bar.arrive 5, %0;" ::"n"(TPB) : "memory"); // BG
     }
+  }
+}
+
+// Persistent pass kernel body: resolves the pass plan (returns at once for a pass that is
+// gated off or skipped), then runs the pass with its launch parameters when the plan keeps
+// them (every pass of a sort that skips none), else with the plan's buffers.
+template <int KB, int VB, int FP, int TPB, int ITEMS, bool STABLE, class Hook = PlainPassHook, size_t EXTRA = 0>
+__device__ __forceinline__ void onesweep_persistent_body(const OnesweepParams& p, const Hook& hook = Hook{})
+{
+  PassIO res;
+  if (!resolve_pass<KB, VB>(p, res))
+  {
+    return; // uniform over the grid
+  }
+  if constexpr (Hook::template digits_t<ITEMS>::computed)
+  {
+    // passes with computed digits (the learned partition) have no plan
+    onesweep_persistent_impl<KB, VB, FP, TPB, ITEMS, STABLE, Hook, EXTRA, false>(p, hook, res);
+    return;
+  }
+  const bool as_launched = res.keys_in == p.keys_in && res.keys_out == p.keys_out && res.values_in == p.values_in
+                        && res.values_out == p.values_out && res.encode_in == p.encode_in
+                        && res.decode_out == p.decode_out;
+  if (as_launched)
+  {
+    onesweep_persistent_impl<KB, VB, FP, TPB, ITEMS, STABLE, Hook, EXTRA, false>(p, hook, res);
+  }
+  else
+  {
+    onesweep_persistent_impl<KB, VB, FP, TPB, ITEMS, STABLE, Hook, EXTRA, true>(p, hook, res);
   }
 }
 

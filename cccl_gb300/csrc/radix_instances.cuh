@@ -19,7 +19,11 @@
   extern "C" __global__ void __launch_bounds__(gb300::ONESWEEP_TPB)                                             \
     gb300_onesweep_dyn_k##KB##_v##VB##_##SUF(const gb300::OnesweepParams p)                                     \
   {                                                                                                             \
-    gb300::onesweep_body<KB, VB, FP, gb300::ONESWEEP_TPB, gb300::onesweep_items(KB, VB), true>(p);              \
+    gb300::OnesweepParams q = p;                                                                                \
+    if (gb300::apply_pass_plan<KB, VB>(q))                                                                      \
+    {                                                                                                           \
+      gb300::onesweep_body<KB, VB, FP, gb300::ONESWEEP_TPB, gb300::onesweep_items(KB, VB), true>(q);            \
+    }                                                                                                           \
   }                                                                                                             \
   extern "C" __global__ void __launch_bounds__(gb300::persistent_tpb(KB, VB), gb300::PERSISTENT_MINB)                                        \
     gb300_onesweep_k##KB##_v##VB##_##SUF(const gb300::OnesweepParams p)                                         \
@@ -45,7 +49,7 @@
   }
 
 #define GB300_HISTOGRAM(KB, FP, SUF)                                                                              \
-  extern "C" __global__ void __launch_bounds__(gb300::HISTOGRAM_TPB)                                            \
+  extern "C" __global__ void __launch_bounds__(gb300::HISTOGRAM_TPB, gb300::HISTOGRAM_MINB)                     \
     gb300_histogram_k##KB##_##SUF(const gb300::HistogramParams p)                                               \
   {                                                                                                             \
     gb300::histogram_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                                     \

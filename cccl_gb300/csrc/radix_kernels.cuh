@@ -44,14 +44,58 @@ __device__ __forceinline__ void init_body(const InitParams& p)
   }
 }
 
+// PLAN_* words of a plain sort's digit passes (see sort_params.h) from the passes whose
+// digit is the same for every key (bit q of trivial_mask). Kept out of line: it runs once
+// per sort, and inlined it cost the histogram kernels registers.
+__device__ __noinline__ void write_pass_plan(uint32_t* plan, int num_passes, int plan_mode, uint32_t trivial_mask)
+{
+  const int P        = num_passes;
+  const uint32_t all = (1u << P) - 1u;
+  uint32_t run       = ~trivial_mask & all; // passes that run
+  const int k0       = __popc(run);
+  const bool extra   = plan_mode == PLAN_MODE_DOUBLE ? ((k0 & 1) != (P & 1)) : (k0 == 0);
+  if (extra)
+  {
+    run |= trivial_mask & (0u - trivial_mask); // the first skippable pass runs too
+  }
+  const int k  = __popc(run);
+  int j        = 0;
+  int prev_dst = 0;
+  for (int q = 0; q < P; ++q)
+  {
+    uint32_t w = PLAN_SKIP;
+    if ((run >> q) & 1u)
+    {
+      int src, dst;
+      if (plan_mode == PLAN_MODE_DOUBLE)
+      {
+        src = j & 1;
+        dst = (j + 1) & 1;
+      }
+      else
+      {
+        src = j == 0 ? 0 : prev_dst;
+        dst = ((k - 1 - j) % 2 == 0) ? 1 : 2; // the last pass writes the output
+      }
+      w = (uint32_t(src) << PLAN_SRC_SHIFT) | (uint32_t(dst) << PLAN_DST_SHIFT) | (j == 0 ? PLAN_ENCODE : 0u)
+        | (j == k - 1 ? PLAN_DECODE : 0u);
+      prev_dst = dst;
+      ++j;
+    }
+    plan[q] = w;
+  }
+}
+
 // Second half of every all-pass histogram kernel: clears pass 0's look-back buffer, adds
 // this CTA's shared counts (sh[pass * 256 + digit]) to the global ones, and the last CTA
-// to finish writes each pass's exclusive prefix (portion 0's digit bases).
+// to finish writes each pass's exclusive prefix (portion 0's digit bases) and, when asked,
+// the pass plan (the PLAN_* words: which passes skip, which buffers the others use).
 template <int TPB>
 __device__ __forceinline__ void histogram_finish(const HistogramParams& p, const uint32_t* sh)
 {
   constexpr int R = RADIX_DIGITS;
   __shared__ uint32_t last_flag;
+  __shared__ uint32_t trivial_mask; // bit q: one digit holds every key in pass q
   const int tid = threadIdx.x;
   // clear the look-back buffer of pass 0
   for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < p.lookback_words;
@@ -72,7 +116,8 @@ __device__ __forceinline__ void histogram_finish(const HistogramParams& p, const
   __syncthreads();
   if (tid == 0)
   {
-    last_flag = (atomicAdd(&p.ctrl->hist_done, 1u) == gridDim.x - 1) ? 1u : 0u;
+    last_flag    = (atomicAdd(&p.ctrl->hist_done, 1u) == gridDim.x - 1) ? 1u : 0u;
+    trivial_mask = 0u;
   }
   __syncthreads();
   if (last_flag == 0)
@@ -111,6 +156,29 @@ __device__ __forceinline__ void histogram_finish(const HistogramParams& p, const
       out[lane * 8 + j] = run;
       run += c[j];
     }
+  }
+  if (p.plan == nullptr)
+  {
+    return;
+  }
+  // a pass is skippable when one digit holds every key (counts re-read: fewer live registers)
+  if (warp < p.num_passes)
+  {
+    bool all_one_digit = false;
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j)
+    {
+      all_one_digit |= __ldcg(&p.ctrl->counts[warp * R + lane * 8 + j]) == p.num_items;
+    }
+    if (__any_sync(0xffffffffu, all_one_digit) && lane == 0)
+    {
+      atomicOr(&trivial_mask, 1u << warp);
+    }
+  }
+  __syncthreads();
+  if (tid == 0)
+  {
+    write_pass_plan(p.plan, p.num_passes, p.plan_mode, trivial_mask);
   }
 }
 

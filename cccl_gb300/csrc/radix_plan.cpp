@@ -247,6 +247,9 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.lookback_clear = lb[0];
     p.lookback_words = t.lookback_words;
     p.gate           = c.gate;
+    // the pass plan: passes whose digit is the same for every key are skipped
+    p.plan      = ctrl->plan;
+    p.plan_mode = c.overwrite ? PLAN_MODE_DOUBLE : PLAN_MODE_SEPARATE;
     const uint64_t want = ceil_div(n, uint64_t(pol.histogram_tpb) * (16 / kb) * 4);
     const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sm_count()) * 4)));
     launch("histogram", ks.histogram, grid, unsigned(pol.histogram_tpb), 0, c.stream, p);
@@ -275,6 +278,11 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     }
   }
   const uint64_t tiles_per_portion = t.portion_items / t.tile_items;
+  // buffer tables of the pass plan (PLAN_MODE_DOUBLE: {current, alternate};
+  // PLAN_MODE_SEPARATE: {input, output, temporary})
+  const void* key_bufs[3]   = {c.keys[0], c.keys[1], c.overwrite ? nullptr : keys_tmp};
+  const void* value_bufs[3] = {has_vals ? c.values[0] : nullptr, has_vals ? c.values[1] : nullptr,
+                               (c.overwrite || !has_vals) ? nullptr : values_tmp};
   for (int p = 0; p < passes; ++p)
   {
     const int bit = c.begin_bit + p * RADIX_BITS;
@@ -304,6 +312,12 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.encode_in     = p == 0;
       op.decode_out    = p == passes - 1;
       op.gate          = c.gate;
+      op.plan          = &ctrl->plan[p];
+      for (int b = 0; b < 3; ++b)
+      {
+        op.key_bufs[b]   = key_bufs[b];
+        op.value_bufs[b] = value_bufs[b];
+      }
       if (persistent)
       {
         const bool order_free =

@@ -758,11 +758,11 @@ __device__ __forceinline__ void seg_device_onesweep_body(const SegDeviceParams& 
     const uint32_t tile_first = local * L::TILE;
     const uint32_t valid      = min(uint32_t(L::TILE), seg.size - tile_first);
     U keys[ITEMS];
-    load_tile_keys_global<KB, TPB, ITEMS>(p, tile_first, valid, keys);
+    load_tile_keys_global<KB, TPB, ITEMS>(p, p.keys_in, p.encode_in, tile_first, valid, keys);
     onesweep_tile<KB, VB, FP, TPB, ITEMS, true>(p, local, valid, keys, whist, gdelta, misc, kstage, vstage, [&](auto& vals) {
       if constexpr (VB > 0)
       {
-        load_tile_values_global<VB, TPB, ITEMS>(p, tile_first, valid, vals);
+        load_tile_values_global<VB, TPB, ITEMS>(p.values_in, tile_first, valid, vals);
       }
     });
   }

@@ -36,8 +36,24 @@ struct SortControl
   uint32_t hist_done;                                   // CTAs finished in the histogram
   uint32_t status;                                      // STATUS_* bits
   uint32_t pad[2];
+  uint32_t plan[MAX_PASSES];                            // PLAN_* word of every digit pass
   // followed by tile counters, one per (pass, portion)
 };
+
+// Pass plan of a plain sort, one word per digit pass, written by the histogram's last CTA.
+// A pass whose digit is the same for every key (one digit holds all n keys) is the identity
+// permutation and is skipped; the passes that run take their buffers in turn, the first of
+// them encodes and the last decodes. When the passes that run would leave the result in
+// another buffer than the one every pass running would (the selector CUB reports), the first
+// skippable pass runs as well (a single-digit pass: its tiles are copied in order).
+constexpr uint32_t PLAN_SKIP       = 1u << 0;
+constexpr uint32_t PLAN_ENCODE     = 1u << 1; // first pass that runs: raw keys are encoded on load
+constexpr uint32_t PLAN_DECODE     = 1u << 2; // last pass that runs: keys are decoded on store
+constexpr int PLAN_SRC_SHIFT       = 8;       // 2-bit index into OnesweepParams::key_bufs / value_bufs
+constexpr int PLAN_DST_SHIFT       = 10;
+constexpr int PLAN_MODE_NONE       = 0;       // no plan: every pass runs as launched
+constexpr int PLAN_MODE_DOUBLE     = 1;       // buffers {current, alternate}: pass j reads j & 1
+constexpr int PLAN_MODE_SEPARATE   = 2;       // buffers {input, output, temporary}: the last pass writes the output
 
 // Optional launch gate of the plain-path kernels: with gate non-null a kernel does its
 // work only if (*gate & gate_mask) != 0, a flag an earlier kernel of the same stream set.
@@ -69,6 +85,9 @@ struct HistogramParams
   uint32_t* lookback_clear;   // look-back buffer of pass 0, zeroed here
   unsigned long long lookback_words;
   KernelGate gate;
+  uint32_t* plan;             // [num_passes] pass plan words to write, or null (no skipping)
+  int plan_mode;              // PLAN_MODE_*
+  int pad0;
 };
 
 struct OnesweepParams
@@ -95,6 +114,13 @@ struct OnesweepParams
   int encode_in;              // first pass: raw keys are encoded on load
   int decode_out;             // last pass: keys are decoded on store
   KernelGate gate;
+  // Pass plan (null: the pass runs with the buffers above). With a plan the pass reads its
+  // PLAN_* word: a skipped pass only clears its rows of lookback_next; a pass that runs
+  // takes keys_in / keys_out / values_in / values_out from these tables by the word's
+  // indices, and encode_in / decode_out from its flags.
+  const uint32_t* plan;
+  const void* key_bufs[3];    // whole arrays
+  const void* value_bufs[3];
 };
 
 struct SingleTileParams

@@ -56,6 +56,9 @@ GB300_HD constexpr int persistent_main(int kb, int vb)
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
 constexpr int HISTOGRAM_TPB    = 512;
+// CTAs per SM the plain histogram's registers are sized for (32 registers a thread): it is
+// bound by shared-memory atomics, and at 40 registers (three CTAs per SM) it ran 20-40 % slower
+constexpr int HISTOGRAM_MINB   = 4;
 
 GB300_HD constexpr int onesweep_items(int kb, int vb)
 {

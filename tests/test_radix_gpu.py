@@ -270,3 +270,55 @@ def test_descending_bit_window_zeros(oracle, dtype, n):
         # 2000 pairs fit CUB's single tile for every key width here (>= 2304 with u32 values)
         rk, rv = oracle.radix_sort(k, I.index_values(n), b, e, True, threads=4, onesweep_zeros=n > 2304)
         assert ko.tobytes() == rk.tobytes() and vo.tobytes() == rv.tobytes()
+
+
+def _trivial_pass_keys(case, n, rng):
+    """Keys whose digit is the same for every key in some 8-bit passes, and the passes that
+    are not: (keys, begin_bit, end_bit)."""
+    if case == "u64_low_half":  # the top four bytes are zero: passes 4-7 skip
+        return I.uniform_bits(np.uint64, n, rng) >> np.uint64(32), 0, 64
+    if case == "u32_byte1_only":  # one pass runs; the parity asks for one more
+        return (rng.integers(0, 256, n).astype(np.uint32) << np.uint32(8)) | np.uint32(0x3C0000A5), 0, 32
+    if case == "u16_high_only":
+        return rng.integers(0, 256, n).astype(np.uint16) << np.uint16(8), 0, 16
+    if case == "u8_all_equal":
+        return np.full(n, 0x5A, np.uint8), 0, 8
+    if case == "u32_all_equal":
+        return np.full(n, 0xDEADBEEF, np.uint32), 0, 32
+    if case == "f64_all_equal":
+        return np.full(n, -2.5, np.float64), 0, 64
+    if case == "f32_signed_zeros":  # +0.0 and -0.0 fold to one digit in every pass
+        return np.where(rng.random(n) < 0.5, np.float32(0.0), np.float32(-0.0)).astype(np.float32), 0, 32
+    if case == "f32_small_integers":  # the low mantissa bytes are zero
+        return rng.integers(-1000, 1000, n).astype(np.float32), 0, 32
+    if case == "u64_window_constant_low":  # bits 8..15 constant inside the window 8..40
+        k = I.uniform_bits(np.uint64, n, rng) & ~np.uint64(0xFF00)
+        return k | np.uint64(0x7700), 8, 40
+    raise ValueError(case)
+
+
+@pytest.mark.parametrize("overwrite", [False, True], ids=["pointers", "double_buffer"])
+@pytest.mark.parametrize(
+    "case",
+    ["u64_low_half", "u32_byte1_only", "u16_high_only", "u8_all_equal", "u32_all_equal", "f64_all_equal",
+     "f32_signed_zeros", "f32_small_integers", "u64_window_constant_low"],
+)
+def test_trivial_passes_skipped(oracle, case, overwrite):
+    """Digit passes whose digit is the same for every key are skipped (the histogram's pass
+    plan); the result, the stable order of equal keys and the DoubleBuffer selector stay
+    CUB's, including when no pass runs and when the parity makes one skippable pass run."""
+    from gpu_util import gpu_sort
+
+    rng = np.random.default_rng(len(case) * 101 + overwrite)
+    for n in (300_001, 1_500_007):  # several tiles per CTA in the larger
+        k, b, e = _trivial_pass_keys(case, n, rng)
+        passes = -(-(e - b) // 8)
+        for desc in (False, True):
+            for vals in (None, I.index_values(n)):
+                ko, vo, sel = gpu_sort(k, vals, b, e, desc, overwrite)
+                rk, rv = oracle.radix_sort(k, vals, b, e, desc, threads=4)
+                assert ko.tobytes() == rk.tobytes(), (case, n, desc, vals is None)
+                if vals is not None:
+                    assert vo.tobytes() == rv.tobytes(), (case, n, desc)
+                if overwrite:
+                    assert sel == passes & 1
