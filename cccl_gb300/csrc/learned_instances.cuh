@@ -43,6 +43,11 @@ extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitPa
   {                                                                                                             \
     gb300::learned_hist_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                                  \
   }                                                                                                             \
+  extern "C" __global__ void __launch_bounds__(gb300::LEARNED_ROUTE_TPB) gb300_learned_route_k##KB##_##FS(      \
+    const gb300::LearnedRouteParams p)                                                                          \
+  {                                                                                                             \
+    gb300::learned_route_body<KB, FP>(p);                                                                       \
+  }                                                                                                             \
   extern "C" __global__ void __launch_bounds__(256) gb300_learned_bounds_k##KB##_##FS(                          \
     const gb300::LearnedBoundsParams p)                                                                         \
   {                                                                                                             \

@@ -271,6 +271,49 @@ __device__ __forceinline__ void learned_cells_body(const LearnedFitParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
+// route: one CTA over the sorted sample. Counts the sample keys that lie in a bucket
+// predicted to overflow and sets the route (LEARNED_ROUTE_*, see sort_params.h).
+// ---------------------------------------------------------------------------------------
+template <int KB, int FP>
+__device__ __forceinline__ void learned_route_body(const LearnedRouteParams& p)
+{
+  using U = typename uint_of<KB>::type;
+  constexpr int PER = LEARNED_SAMPLE / LEARNED_ROUTE_TPB;
+  __shared__ LearnedTables<U> tables;
+  __shared__ uint32_t in_large;
+  learned_load_tables<U>(p.model, &tables, p.bucket_log2);
+  if (threadIdx.x == 0)
+  {
+    in_large = 0u;
+  }
+  __syncthreads();
+  const U* s           = static_cast<const U*>(p.sorted_sample);
+  const int range_log2 = learned_range_log2(p.bucket_log2);
+  const uint32_t bmax  = (1u << p.bucket_log2) - 1u;
+  uint32_t count       = 0;
+  for (int j = 0; j < PER; ++j)
+  {
+    const int i = int(threadIdx.x) * PER + j;
+    if (i + p.span < LEARNED_SAMPLE)
+    {
+      const uint32_t b0 = learned_bucket<U, FP>(s[i], tables, range_log2, bmax);
+      const uint32_t b1 = learned_bucket<U, FP>(s[i + p.span], tables, range_log2, bmax);
+      count += b0 == b1 ? 1u : 0u;
+    }
+  }
+  count = __reduce_add_sync(0xffffffffu, count);
+  if ((threadIdx.x & 31) == 0)
+  {
+    atomicAdd(&in_large, count);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    p.model->route = 2u * in_large > uint32_t(LEARNED_SAMPLE) ? LEARNED_ROUTE_PLAIN : LEARNED_ROUTE_LEARNED;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // hist: digit counts of every partition pass in one read of the keys
 // ---------------------------------------------------------------------------------------
 template <int KB, int FP, int TPB>
@@ -280,6 +323,10 @@ __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
   constexpr int R = RADIX_DIGITS;
   __shared__ uint32_t sh[MAX_PASSES * R];
   __shared__ LearnedTables<U> tables;
+  if (!gate_open(p.h.gate))
+  {
+    return;
+  }
 
   for (int i = threadIdx.x; i < MAX_PASSES * R; i += TPB)
   {
@@ -368,6 +415,10 @@ template <int KB, int FP>
 __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p)
 {
   using U = typename uint_of<KB>::type;
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
   __shared__ LearnedTables<U> tables;
   learned_load_tables<U>(p.model, &tables, p.bucket_log2);
   __syncthreads();
@@ -452,6 +503,10 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
   constexpr int NW   = TPB / 32;
   constexpr int PER  = CAP / TPB; // keys per thread
   static_assert(CAP % TPB == 0 && CAP < 65536, "16-bit bin fields and indices");
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
 
   extern __shared__ __align__(16) unsigned char smem[];
   U* kraw        = reinterpret_cast<U*>(smem + L::kraw_off);

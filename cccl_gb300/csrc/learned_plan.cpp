@@ -10,6 +10,7 @@
 #include "learned_plan.h"
 
 #include <algorithm>
+#include <cstddef>
 
 #include "abi_common.h"
 #include "sort_policy.h"
@@ -112,15 +113,15 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
   off += align_up(t.sample_temp_bytes, 256);
   t.bounds_off = off;
   off += 256 + align_up(3 * 8 * (size_t(1) << t.bucket_log2), 256); // counters; begins, ends, rest_ends
-  t.keys_tmp_off = off;
-  if (!c.overwrite)
+  // The plain route's temporary storage. Without overwrite it holds alternate key and value
+  // buffers of n items, which the learned passes use as their own (only one route runs).
   {
-    off += align_up(size_t(n) * kb, 256);
-  }
-  t.values_tmp_off = off;
-  if (!c.overwrite && has_vals)
-  {
-    off += align_up(size_t(n) * vb, 256);
+    const RadixTempPlan pt = plan_radix_temp(s.plain_pol, n, 0, 8 * kb, !c.overwrite, true);
+    t.plain_off            = off;
+    t.plain_bytes          = pt.total_bytes;
+    t.keys_tmp_off         = t.plain_off + pt.keys_tmp_off;
+    t.values_tmp_off       = t.plain_off + pt.values_tmp_off;
+    off += align_up(t.plain_bytes, 256);
   }
   t.seg_off = off;
   // the buffer the bucket sort must land in changes its pass count: size for both
@@ -245,6 +246,18 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     launch("learned_fit", s.lk.fit, unsigned(LEARNED_LEAVES), unsigned(LEARNED_FIT_TPB), 0, c.stream, p);
     launch("learned_cells", s.lk.cells, unsigned(ceil_div(LEARNED_CELLS + 1, 256)), 256, 0, c.stream, p);
   }
+  // 4b. the route: the learned kernels below run only on LEARNED_ROUTE_LEARNED, the plain
+  // sort at the end only on LEARNED_ROUTE_PLAIN (a flag on the device: no host sync)
+  {
+    LearnedRouteParams p{};
+    p.sorted_sample = sample[ssel];
+    p.model         = model;
+    p.bucket_log2   = t.bucket_log2;
+    p.span          = int(std::max<uint64_t>(1, ceil_div(uint64_t(t.bucket_cap) * LEARNED_SAMPLE, n)));
+    launch("learned_route", s.lk.route, 1, unsigned(LEARNED_ROUTE_TPB), 0, c.stream, p);
+  }
+  const KernelGate learned_gate{&model->route, LEARNED_ROUTE_LEARNED, 0};
+  const KernelGate plain_gate{&model->route, LEARNED_ROUTE_PLAIN, 0};
   // 5. digit counts of every partition pass (and pass 0's look-back cleared)
   {
     LearnedHistParams p{};
@@ -259,6 +272,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     p.h.bins           = bins;
     p.h.lookback_clear = lb[0];
     p.h.lookback_words = t.lookback_words;
+    p.h.gate           = learned_gate;
     p.model            = model;
     p.bucket_log2      = t.bucket_log2;
     const uint64_t want = ceil_div(n, uint64_t(HISTOGRAM_TPB) * (16 / kb) * 4);
@@ -319,6 +333,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
       op.num_bits         = std::min(RADIX_BITS, t.bucket_log2 - q * RADIX_BITS);
       op.encode_in        = q == 0;
       op.decode_out       = q == P - 1;
+      op.gate             = learned_gate;
       lp.model            = model;
       lp.bucket_log2      = t.bucket_log2;
       lp.digit_shift      = q * RADIX_BITS;
@@ -328,11 +343,13 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
   }
   void* part_keys = kdst[P - 1];
   void* part_vals = has_vals ? vdst[P - 1] : nullptr;
-  // 7. begin and end of every bucket, from one read of the partitioned keys
+  // 7. begin and end of every bucket, from one read of the partitioned keys. The counters and
+  // all three bound arrays are cleared on either route: on the plain route every bucket stays
+  // empty, so the segmented sort below has nothing to do
   {
     InitParams z{};
-    z.words     = bucket_ctrs; // the counters, begins and ends
-    z.num_words = 64 + 4 * (uint64_t(1) << t.bucket_log2);
+    z.words     = bucket_ctrs; // the counters, begins, ends and rest_ends
+    z.num_words = 64 + 6 * (uint64_t(1) << t.bucket_log2);
     launch("learned_init", s.lk.init, unsigned(std::min<uint64_t>(ceil_div(z.num_words, 256), uint64_t(sms) * 8)),
            256, 0, c.stream, z);
     LearnedBoundsParams p{};
@@ -343,6 +360,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     p.ends        = ends;
     p.codec       = codec;
     p.bucket_log2 = t.bucket_log2;
+    p.gate        = learned_gate;
     const uint64_t warps = ceil_div(n, 32ull * learned_bounds_items(kb));
     const unsigned grid  = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(warps, 8), uint64_t(sms) * 16)));
     launch("learned_bounds", s.lk.bounds, grid, 256, 0, c.stream, p);
@@ -370,6 +388,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
       bp.num_buckets = uint32_t(1u << t.bucket_log2);
       bp.num_items   = n;
       bp.codec       = codec;
+      bp.gate        = learned_gate;
       const CUkernel k    = t.bucket_cap == 4096 ? s.lk.bucket4k : s.lk.bucket8k;
       const int tpb       = learned_bucket_tpb(t.bucket_cap);
       const size_t smem   = learned_bucket_smem(kb, vb, t.bucket_cap);
@@ -415,6 +434,27 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
       radix_sort_dispatch(s.plain_pol, s.plain_ks, fc, &fsel);
     }
   }
+  // 10. the plain route: the plain radix sort of the input, where the learned sort puts its
+  // result (the same buffer and selector)
+  {
+    RadixCall pc{};
+    pc.keys[0]            = c.keys[0];
+    pc.keys[1]            = c.keys[1];
+    pc.values[0]          = has_vals ? c.values[0] : nullptr;
+    pc.values[1]          = has_vals ? c.values[1] : nullptr;
+    pc.num_items          = n;
+    pc.begin_bit          = 0;
+    pc.end_bit            = 8 * kb;
+    pc.overwrite          = c.overwrite;
+    pc.descending         = c.descending;
+    pc.d_temp_storage     = base + t.plain_off;
+    size_t pbytes         = t.plain_bytes;
+    pc.temp_storage_bytes = &pbytes;
+    pc.stream             = c.stream;
+    pc.gate               = plain_gate;
+    int psel              = 0;
+    radix_sort_dispatch(s.plain_pol, s.plain_ks, pc, &psel);
+  }
   *selector = final_sel;
 }
 
@@ -429,6 +469,16 @@ LearnedStats learned_sort_stats(const LearnedSetup& s, const RadixCall& c)
   }
   st.bucket_log2      = t.bucket_log2;
   st.partition_passes = t.passes;
+  uint32_t route      = 0;
+  check(cuMemcpyDtoH(&route,
+                     CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.model_off + offsetof(LearnedModel, route)),
+                     sizeof(route)),
+        "cuMemcpyDtoH(learned route)");
+  if (route != LEARNED_ROUTE_LEARNED)
+  {
+    st.learned = 0; // the model sent this input to the plain radix sort
+    return st;
+  }
   uint32_t w[SEG_CTR_WORDS];
   check(cuMemcpyDtoH(w, CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.seg_off), sizeof(w)),
         "cuMemcpyDtoH(learned stats)");

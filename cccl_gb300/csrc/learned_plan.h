@@ -23,6 +23,7 @@ struct LearnedKernels
   CUkernel sample;
   CUkernel fit;
   CUkernel cells;
+  CUkernel route; // learned or plain, from the model and the sorted sample
   CUkernel hist;
   CUkernel pass;
   CUkernel bounds;
@@ -63,6 +64,10 @@ struct LearnedTempPlan
   // n >= 2^30: a bucket may reach the segmented sort's 2^30-key limit; a plain radix sort of
   // the partitioned keys, gated on the segmented sort's bad-segment flag, then redoes the sort
   size_t fallback_off, fallback_bytes;
+  // the plain route: the plain radix sort of the input, gated on the route word. Without
+  // overwrite its alternate key/value buffers are the learned passes' (keys_tmp_off and
+  // values_tmp_off point into this region): only one of the two routes runs
+  size_t plain_off, plain_bytes;
   size_t total_bytes;
 };
 

@@ -187,6 +187,7 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
     s->lk.sample = get_kernel(r.learned_library, "gb300_learned_sample_k" + k + "_" + fs);
     s->lk.fit    = get_kernel(r.learned_library, "gb300_learned_fit_k" + k);
     s->lk.cells  = get_kernel(r.learned_library, "gb300_learned_cells_k" + k);
+    s->lk.route  = get_kernel(r.learned_library, "gb300_learned_route_k" + k + "_" + fs);
     s->lk.hist   = get_kernel(r.learned_library, "gb300_learned_hist_k" + k + "_" + fs);
     s->lk.pass   = get_kernel(r.learned_library, "gb300_learned_pass_k" + k + "_v" + std::to_string(vb) + "_" + fs);
     s->lk.bounds = get_kernel(r.learned_library, "gb300_learned_bounds_k" + k + "_" + fs);

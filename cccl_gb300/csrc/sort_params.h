@@ -264,8 +264,27 @@ struct LearnedModel
   float icpt[LEARNED_LEAVES];
   unsigned long long kmin;
   int shift;
-  int pad0;
+  uint32_t route; // LEARNED_ROUTE_*: written after the fit, the gate of both routes' kernels
   unsigned char cell_leaf[LEARNED_CELLS + 16]; // [LEARNED_CELLS + 1] used
+};
+
+// Route of one learned sort, chosen on the device from the fitted model and the sorted
+// sample s. Each sample key stands for n / 2^16 keys, so a bucket holding more than
+// span = ceil(cap * 2^16 / n) sample keys is predicted to exceed cap, the largest bucket the
+// bucket sort takes; bucket ids never decrease along s, so bucket(s[i]) == bucket(s[i + span])
+// says key i lies in such a bucket. When more than half of the sample does, the partition
+// cannot pay and the plain radix sort runs instead (all-equal and near-constant keys, heavy
+// duplicates).
+constexpr uint32_t LEARNED_ROUTE_LEARNED = 1u;
+constexpr uint32_t LEARNED_ROUTE_PLAIN   = 2u;
+constexpr int LEARNED_ROUTE_TPB         = 1024; // one CTA, 64 sample keys a thread
+
+struct LearnedRouteParams
+{
+  const void* sorted_sample;
+  LearnedModel* model;
+  int bucket_log2;
+  int span; // >= 1
 };
 
 struct LearnedSampleParams
@@ -315,6 +334,7 @@ struct LearnedBucketParams
   uint32_t pad0;
   unsigned long long num_items;  // of the whole array (bounds the L2 prefetches)
   KeyCodec codec;
+  KernelGate gate;
 };
 
 struct LearnedBoundsParams
@@ -327,6 +347,7 @@ struct LearnedBoundsParams
   KeyCodec codec;
   int bucket_log2;
   int pad0;
+  KernelGate gate;
 };
 
 } // namespace gb300
