@@ -16,7 +16,11 @@
  *
  * Keys: 4- and 8-byte integer and floating-point types; values: none, 4 or 8 bytes. Inputs
  * the learned path does not take (fewer than 2^20 keys, a bit window narrower than the key,
- * buffers not 16-byte aligned) are sorted by the plain radix sort.
+ * buffers not 16-byte aligned) are sorted by the plain radix sort. So are inputs the model
+ * predicts the partition cannot pay for: after the fit, a kernel checks how much of the
+ * sorted sample lies in buckets predicted to overflow the bucket sort, and above half
+ * (near-constant keys, heavy duplicates) the plain sort runs instead. The choice is made on
+ * the device, without a host synchronisation, and the result and selector are the same.
  */
 #pragma once
 
@@ -52,7 +56,7 @@ typedef struct cccl_gb300_learned_sort_build_result_t
 /* What the last run did, read back from its temporary storage. */
 typedef struct cccl_gb300_learned_sort_stats_t
 {
-  int learned;             /* 0: the plain radix sort ran */
+  int learned;             /* 0: the plain radix sort ran (input not taken, or routed to it on the device) */
   int bucket_log2;         /* log2 of the number of buckets */
   int partition_passes;    /* stable passes on the bucket id */
   uint32_t block_buckets;  /* non-empty buckets sorted in shared memory */
