@@ -16,6 +16,7 @@ Groups:
   onesweep  persistent onesweep pass (plain sort): u64+u32 pairs, f32+u32 pairs, u32 keys
   block     segmented block classes: ~4096-key segments, f32+i32 and f64+i64
   segpass   segmented device-class pass: lognormal segments, f32+i32 and f64+i64
+  writeout  the pass write-out with and without 32-bit positions (the onesweep group's cases)
 """
 
 from __future__ import annotations
@@ -45,6 +46,10 @@ CANDIDATES = {
         "-DGB300_SEG_BLOCK_ALGO=0 -DGB300_SEG_BLOCK_L_ITEMS=16 -DGB300_SEG_BLOCK_MINB=2",
         "-DGB300_SEG_BLOCK_ALGO=0 -DGB300_SEG_BLOCK_L_ITEMS=8 -DGB300_SEG_BLOCK_MINB=1",
         "-DGB300_SEG_BLOCK_ALGO=1 -DGB300_SEG_BLOCK_L_ITEMS=8 -DGB300_SEG_BLOCK_MINB=1",
+    ],
+    "writeout": [
+        "",
+        "-DGB300_WRITE_OUT_SPECIALISED=0",
     ],
     "segpass": [
         "",
@@ -97,7 +102,7 @@ def measure(group):
     import bench
 
     out = {}
-    if group == "onesweep":
+    if group in ("onesweep", "writeout"):
         n = 1 << 26
         cases = {
             "u64+u32": (bench.make_inputs(torch, n, "u64"), True),

@@ -143,6 +143,13 @@ __device__ __forceinline__ bool apply_pass_plan(OnesweepParams& q)
   return true;
 }
 
+// Compile-time flag carried by a value (for generic lambdas).
+template <bool B>
+struct BoolTag
+{
+  static constexpr bool value = B;
+};
+
 // Decoupled look-back of digit d for `tile` (tile > 0): the sum of the predecessors'
 // counts back to the nearest inclusive prefix. BATCH predecessor rows are read per step (one
 // L2 round trip): inclusive prefixes spread from tile to tile at about BATCH tiles per round
@@ -674,12 +681,19 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
     // Consecutive staging slots of one digit go to consecutive outputs. Every store is
     // bounds-checked against the output size, so even corrupted offsets (a look-back that
     // gave up) cannot write outside the caller's buffers.
-    auto write_out = [&](int b, uint32_t valid) {
+    // The loop is specialised at compile time on the decode (last pass only) and on the
+    // position width: 32-bit positions when the whole array has fewer than 2^31 items.
+#ifndef GB300_WRITE_OUT_SPECIALISED
+#  define GB300_WRITE_OUT_SPECIALISED 1
+#endif
+    auto write_out_as = [&](int b, uint32_t valid, auto decode_tag, auto narrow_tag) {
+      constexpr bool DECODE              = decltype(decode_tag)::value;
+      constexpr bool NARROW              = decltype(narrow_tag)::value;
       const U* ks                        = kbuf(b);
       const V* vs                        = vbuf(b);
       const bool full                    = valid == uint32_t(TILE);
-      const bool decode                  = (FROM_PLAN ? io->decode_out : p.decode_out) != 0;
       const unsigned long long out_limit = misc[2] != 0u ? 0ull : p.num_items_total;
+      const int32_t* gdelta32            = reinterpret_cast<const int32_t*>(gdelta); // low words
 #pragma unroll
       for (int j = 0; j < ITEMS; ++j)
       {
@@ -696,17 +710,71 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
           {
             d = extract_digit<U, FP>(k, bit, dmask);
           }
-          const long long g = gdelta[d] + (long long) s;
-          if ((unsigned long long) g < out_limit)
+          const U out = DECODE ? decode_key<U>(k, p.codec) : k;
+          if constexpr (NARROW)
           {
-            __stcs(kout + g, decode ? decode_key<U>(k, p.codec) : k);
-            if constexpr (VB > 0)
+            // positions and deltas fit in 31 bits; a corrupted delta wraps above the limit
+            const uint32_t g = uint32_t(gdelta32[2 * d] + int32_t(s));
+            if (g < uint32_t(out_limit))
             {
-              __stcs(vout + g, vs[s]);
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vs[s]);
+              }
+            }
+          }
+          else
+          {
+            const long long g = gdelta[d] + (long long) s;
+            if ((unsigned long long) g < out_limit)
+            {
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vs[s]);
+              }
             }
           }
         }
       }
+    };
+    auto write_out = [&](int b, uint32_t valid) {
+      const bool decode = (FROM_PLAN ? io->decode_out : p.decode_out) != 0;
+#if GB300_WRITE_OUT_SPECIALISED
+      const bool narrow = p.num_items_total < (1ull << 31);
+      if (decode)
+      {
+        if (narrow)
+        {
+          write_out_as(b, valid, BoolTag<true>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out_as(b, valid, BoolTag<true>{}, BoolTag<false>{});
+        }
+      }
+      else
+      {
+        if (narrow)
+        {
+          write_out_as(b, valid, BoolTag<false>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out_as(b, valid, BoolTag<false>{}, BoolTag<false>{});
+        }
+      }
+#else
+      if (decode)
+      {
+        write_out_as(b, valid, BoolTag<true>{}, BoolTag<false>{});
+      }
+      else
+      {
+        write_out_as(b, valid, BoolTag<false>{}, BoolTag<false>{});
+      }
+#endif
     };
 
     uint32_t parity     = 0; // bit b: phase parity to wait for on buffer b
