@@ -50,6 +50,13 @@ struct OnesweepSmem
 // CTA, [3] single-digit tile flag and digit, [8..15] scan scratch, [16..19] two mbarriers
 // (persistent kernel).
 
+// Compile-time flag carried by a value (for generic lambdas).
+template <bool B>
+struct BoolTag
+{
+  static constexpr bool value = B;
+};
+
 // Where a pass takes its digits from.
 //   RadixDigits: bits [current_bit, current_bit + num_bits) of the encoded key, recomputed
 //     wherever needed (histogram, ranking, write-out);
@@ -142,13 +149,6 @@ __device__ __forceinline__ bool apply_pass_plan(OnesweepParams& q)
   q.decode_out = io.decode_out;
   return true;
 }
-
-// Compile-time flag carried by a value (for generic lambdas).
-template <bool B>
-struct BoolTag
-{
-  static constexpr bool value = B;
-};
 
 // Decoupled look-back of digit d for `tile` (tile > 0): the sum of the predecessors'
 // counts back to the nearest inclusive prefix. BATCH predecessor rows are read per step (one
@@ -384,32 +384,86 @@ __device__ __forceinline__ void onesweep_tile(
     // Every store is bounds-checked against the output size, so even corrupted offsets
     // (a look-back that gave up) cannot write outside the caller's buffers.
     const unsigned long long out_limit = misc[1] != 0u ? 0ull : out_limit_early;
+    // keys of up to 4 bytes: decode and position width fixed at compile time (as in the
+    // persistent kernel's write-out)
+    auto write_out = [&](auto decode_tag, auto narrow_tag) {
+      constexpr bool DECODE = decltype(decode_tag)::value;
+      constexpr bool NARROW = decltype(narrow_tag)::value;
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j)
-    {
-      const uint32_t s = j * TPB + threadIdx.x;
-      if (full || s < valid)
+      for (int j = 0; j < ITEMS; ++j)
       {
-        const U k = kstage[s];
-        uint32_t d;
-        if constexpr (Digits::computed)
+        const uint32_t s = j * TPB + threadIdx.x;
+        if (full || s < valid)
         {
-          d = dg.stage[s];
-        }
-        else
-        {
-          d = extract_digit<U, FP>(k, bit, dmask);
-        }
-        const long long g = gdelta[d] + (long long) s;
-        if ((unsigned long long) g < out_limit)
-        {
-          __stcs(kout + g, p.decode_out ? decode_key<U>(k, p.codec) : k);
-          if constexpr (VB > 0)
+          const U k = kstage[s];
+          uint32_t d;
+          if constexpr (Digits::computed)
           {
-            __stcs(vout + g, vstage[s]);
+            d = dg.stage[s];
+          }
+          else
+          {
+            d = extract_digit<U, FP>(k, bit, dmask);
+          }
+          const U out = KB <= 4 ? (DECODE ? decode_key<U>(k, p.codec) : k)
+                                : (p.decode_out ? decode_key<U>(k, p.codec) : k);
+          if constexpr (NARROW)
+          {
+            // positions and deltas fit in 31 bits; a corrupted delta wraps above the limit
+            const uint32_t g = uint32_t(reinterpret_cast<const int32_t*>(gdelta)[2 * d] + int32_t(s));
+            if (g < uint32_t(out_limit))
+            {
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vstage[s]);
+              }
+            }
+          }
+          else
+          {
+            const long long g = gdelta[d] + (long long) s;
+            if ((unsigned long long) g < out_limit)
+            {
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vstage[s]);
+              }
+            }
           }
         }
       }
+    };
+    if constexpr (KB <= 4)
+    {
+      const bool narrow = p.num_items_total < (1ull << 31);
+      if (p.decode_out)
+      {
+        if (narrow)
+        {
+          write_out(BoolTag<true>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out(BoolTag<true>{}, BoolTag<false>{});
+        }
+      }
+      else
+      {
+        if (narrow)
+        {
+          write_out(BoolTag<false>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out(BoolTag<false>{}, BoolTag<false>{});
+        }
+      }
+    }
+    else
+    {
+      write_out(BoolTag<false>{}, BoolTag<false>{}); // the decode is chosen per key
     }
   }
 }
