@@ -23,6 +23,7 @@
 //    so no memset runs between passes.
 #pragma once
 
+#include "sort_policy.h"
 #include "tile_rank.cuh"
 
 namespace gb300
@@ -44,46 +45,11 @@ __device__ __forceinline__ void init_body(const InitParams& p)
   }
 }
 
-// PLAN_* words of a plain sort's digit passes (see sort_params.h) from the passes whose
-// digit is the same for every key (bit q of trivial_mask). Kept out of line: it runs once
-// per sort, and inlined it cost the histogram kernels registers.
+// The pass plan (plan_pass_words), kept out of line: it runs once per sort, and inlined it
+// cost the histogram kernels registers.
 __device__ __noinline__ void write_pass_plan(uint32_t* plan, int num_passes, int plan_mode, uint32_t trivial_mask)
 {
-  const int P        = num_passes;
-  const uint32_t all = (1u << P) - 1u;
-  uint32_t run       = ~trivial_mask & all; // passes that run
-  const int k0       = __popc(run);
-  const bool extra   = plan_mode == PLAN_MODE_DOUBLE ? ((k0 & 1) != (P & 1)) : (k0 == 0);
-  if (extra)
-  {
-    run |= trivial_mask & (0u - trivial_mask); // the first skippable pass runs too
-  }
-  const int k  = __popc(run);
-  int j        = 0;
-  int prev_dst = 0;
-  for (int q = 0; q < P; ++q)
-  {
-    uint32_t w = PLAN_SKIP;
-    if ((run >> q) & 1u)
-    {
-      int src, dst;
-      if (plan_mode == PLAN_MODE_DOUBLE)
-      {
-        src = j & 1;
-        dst = (j + 1) & 1;
-      }
-      else
-      {
-        src = j == 0 ? 0 : prev_dst;
-        dst = ((k - 1 - j) % 2 == 0) ? 1 : 2; // the last pass writes the output
-      }
-      w = (uint32_t(src) << PLAN_SRC_SHIFT) | (uint32_t(dst) << PLAN_DST_SHIFT) | (j == 0 ? PLAN_ENCODE : 0u)
-        | (j == k - 1 ? PLAN_DECODE : 0u);
-      prev_dst = dst;
-      ++j;
-    }
-    plan[q] = w;
-  }
+  plan_pass_words(plan, num_passes, plan_mode, trivial_mask);
 }
 
 // Second half of every all-pass histogram kernel: clears pass 0's look-back buffer, adds

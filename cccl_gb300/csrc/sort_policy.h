@@ -133,6 +133,57 @@ GB300_HD constexpr unsigned long long persistent_tile_items(int tpb, int items)
   return (unsigned long long) (tpb - LOOKBACK_THREADS) * items;
 }
 
+// PLAN_* words of a plain sort's digit passes (see sort_params.h) from the passes whose
+// digit is the same for every key (bit q of trivial_mask). Runs on the device (one thread
+// of the histogram's last CTA) and on the host (the CPU test of every mask).
+GB300_HD inline void plan_pass_words(uint32_t* plan, int num_passes, int plan_mode, uint32_t trivial_mask)
+{
+  auto popcount = [](uint32_t x) {
+    int c = 0;
+    for (; x != 0u; x &= x - 1u)
+    {
+      ++c;
+    }
+    return c;
+  };
+  const int P        = num_passes;
+  const uint32_t all = (1u << P) - 1u;
+  trivial_mask &= all;
+  uint32_t run     = ~trivial_mask & all; // passes that run
+  const int k0     = popcount(run);
+  const bool extra = plan_mode == PLAN_MODE_DOUBLE ? ((k0 & 1) != (P & 1)) : (k0 == 0);
+  if (extra)
+  {
+    run |= trivial_mask & (0u - trivial_mask); // the first skippable pass runs too
+  }
+  const int k  = popcount(run);
+  int j        = 0;
+  int prev_dst = 0;
+  for (int q = 0; q < P; ++q)
+  {
+    uint32_t w = PLAN_SKIP;
+    if ((run >> q) & 1u)
+    {
+      int src, dst;
+      if (plan_mode == PLAN_MODE_DOUBLE)
+      {
+        src = j & 1;
+        dst = (j + 1) & 1;
+      }
+      else
+      {
+        src = j == 0 ? 0 : prev_dst;
+        dst = ((k - 1 - j) % 2 == 0) ? 1 : 2; // the last pass writes the output
+      }
+      w = (uint32_t(src) << PLAN_SRC_SHIFT) | (uint32_t(dst) << PLAN_DST_SHIFT) | (j == 0 ? PLAN_ENCODE : 0u)
+        | (j == k - 1 ? PLAN_DECODE : 0u);
+      prev_dst = dst;
+      ++j;
+    }
+    plan[q] = w;
+  }
+}
+
 GB300_HD constexpr int single_tile_capacity()
 {
   return SINGLE_TILE_TPB * SINGLE_TILE_ITEMS;
