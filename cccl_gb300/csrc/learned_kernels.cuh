@@ -408,7 +408,8 @@ __device__ __forceinline__ void learned_pass_body(const LearnedPassParams& p)
 // ends at n. Empty buckets keep the zeros they were cleared to (begin == end). Warp w covers keys
 // [w * 32 * ITEMS, (w + 1) * 32 * ITEMS), lane l the keys l, l + 32, ...; the bucket of the
 // key before each comes from the neighbouring lane. A warp's keys are all loaded before the
-// first is used (ITEMS = learned_bounds_items: as many loads in flight as registers allow).
+// first is used (ITEMS = learned_bounds_items: as many loads in flight as registers allow);
+// a chunk whose first and last keys share the bucket of the key before it is skipped unread.
 // ---------------------------------------------------------------------------------------
 
 template <int KB, int FP>
@@ -438,6 +439,22 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
        w * chunk < n; w += warps_total)
   {
     const unsigned long long first = w * chunk;
+    const unsigned long long last  = (first + chunk < n ? first + chunk : n) - 1;
+    // Buckets of the key before the chunk (none before index 0), of its first and of its
+    // last key, one lane each. Bucket ids never decrease along the keys, so when the three
+    // agree no bucket starts or ends inside the chunk and its keys need not be read.
+    long long probe = -1;
+    if (lane < 3 && !(lane == 0 && first == 0))
+    {
+      probe = (long long) bucket_at(lane == 0 ? first - 1 : lane == 1 ? first : last);
+    }
+    long long carry      = __shfl_sync(0xffffffffu, probe, 0);
+    const long long b_lo = __shfl_sync(0xffffffffu, probe, 1);
+    const long long b_hi = __shfl_sync(0xffffffffu, probe, 2);
+    if (carry == b_lo && b_lo == b_hi && last != n - 1)
+    {
+      continue;
+    }
     // the chunk's keys are loaded before any is used, so their loads overlap
     U k[ITEMS];
 #pragma unroll
@@ -446,8 +463,6 @@ __device__ __forceinline__ void learned_bounds_body(const LearnedBoundsParams& p
       const unsigned long long i = first + (unsigned long long) it * 32 + lane;
       k[it]                      = i < n ? __ldcs(keys + i) : U(0);
     }
-    // bucket of the key before this warp's chunk (none before index 0)
-    long long carry = first == 0 ? -1ll : (long long) bucket_at(first - 1);
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it)
     {
