@@ -214,7 +214,7 @@ def kernel_times(torch, sorter, steps):
 
 
 def segmented_workload(seed=77, total=1 << 27):
-    """BASELINE's batched configuration: f32 N(0,1) keys, 0.1% set to +-0.0/NaN, i32 values,
+    """The batched segmented-sort configuration: f32 N(0,1) keys, 0.1% set to +-0.0/NaN, i32 values,
     lognormal(5, 2.5) segment lengths clipped to [1, 2^23], 5% empty, int32 offsets."""
     import numpy as np
 

@@ -1,4 +1,4 @@
-"""Seeded segment layouts (BASELINE's batched-sort configuration and the edge cases of the
+"""Seeded segment layouts (the batched segmented-sort configuration and the edge cases of the
 reference's segmented-sort tests, c/parallel/test/test_segmented_sort.cpp:593-724)."""
 
 from __future__ import annotations
