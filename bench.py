@@ -162,6 +162,18 @@ class Sorter:
         return self.passes * self.n * 2 * (self.key_bytes + self.value_bytes)
 
 
+def job_throughput(torch, ms, items_per_rank, world, device):
+    """The slowest rank's time per step (max over ranks) and the whole job's throughput: the
+    items all ranks sorted per step divided by that time. Ranks run independent replicas."""
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    slowest = float(t.item())
+    return slowest, world * items_per_rank / (slowest / 1000.0)
+
+
 def time_steps(torch, fn, steps, warmup, barrier):
     for _ in range(warmup):
         fn()
@@ -557,13 +569,7 @@ def run_engine(args):
 
     with ClockSampler(local) as clocks:
         ms = time_steps(torch, main.run, args.steps, args.warmup, barrier)
-    ms_t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = world * n / (ms / 1000.0)
+    ms, value = job_throughput(torch, ms, n, world, "cuda")
 
     # per-kernel durations (observer run, separate from the timed steps)
     ktimes, launches = kernel_times(torch, main, max(3, args.steps // 2))
