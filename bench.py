@@ -19,7 +19,11 @@ between steps. Reported beside the headline line:
     lognormal/uniform mix, all-equal, sorted-then-reversed), bit-exactness checked.
 
 Metric: sorted keys per second (higher is better); roofline on HBM with algorithmic bytes
-= passes x N x 2 x (key + value bytes).
+= passes x N x 2 x (key + value bytes). Rows whose digit passes were skipped (constant
+digits move no bytes) print a null roofline. "verified": the headline result checked on
+the GPU after the timed steps (keys in order, equal keys in index order, values a
+permutation of the indices naming their keys); the learned rows check the plain result
+the same way ("plain_verified").
 
 --impl reference times the reference library's CPU sort (thrust::sort_by_key on its
 OpenMP backend, from the toolkit's CCCL headers) on a bounded sample of the workload.
@@ -41,6 +45,13 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "tests"))
+
+
+def check_sorted_pairs(*args, **kw):
+    """GPU-side check of a pairs sort with index values (tests/gpu_util.py)."""
+    from gpu_util import check_sorted_pairs as check
+
+    return check(*args, **kw)
 
 N_LOG2 = 28
 METRIC = "sorted keys/s (SortPairs 2^28 u64 keys + u32 values, 1 GB300)"
@@ -160,6 +171,23 @@ class Sorter:
 
     def algorithmic_bytes(self):
         return self.passes * self.n * 2 * (self.key_bytes + self.value_bytes)
+
+
+def passes_that_run(torch, keys, begin_bit=0, end_bit=None):
+    """The 8-bit digit passes of [begin_bit, end_bit) whose digit is not the same for every
+    key (the others are skipped by the sort's pass plan and move no bytes). Floats fold -0.0
+    into +0.0 first, as the sort's digit extraction does."""
+    size = keys.element_size()
+    raw = keys.view({1: torch.int8, 2: torch.int16, 4: torch.int32, 8: torch.int64}[size]).long()
+    if keys.dtype in (torch.float16, torch.float32, torch.float64):
+        neg_zero = (-(1 << (8 * size - 1))) if size == 8 else (1 << (8 * size - 1))
+        raw = torch.where(raw == neg_zero, torch.zeros_like(raw), raw)
+    end_bit = 8 * size if end_bit is None else end_bit
+    run = 0
+    for bit in range(begin_bit, end_bit, 8):
+        d = (raw >> bit) & ((1 << min(8, end_bit - bit)) - 1)
+        run += int(bool((d != d[0]).any()))
+    return run
 
 
 def job_throughput(torch, ms, items_per_rank, world, device):
@@ -427,10 +455,16 @@ def run_learned(torch, reps):
         lk, lv, lsel = results["learned"]
         res["bitexact_vs_plain"] = bool(torch.equal(pk.view(torch.uint8), lk.view(torch.uint8))
                                         and torch.equal(pv, lv) and psel == lsel)
+        # the plain result itself against an independent check (order, stability, permutation)
+        res["plain_verified"] = check_sorted_pairs(k0, pk, pv, "f")
+        full_passes = 8 * kb // 8
+        res["plain_passes_run"] = passes_that_run(torch, k0)
         res["speedup_vs_plain"] = res["plain_ms"] / res["learned_ms"]
         plain_bytes = (8 * kb // 8) * n * 2 * (kb + vb)  # 8-bit passes x N x 2 x (K + V)
+        # a fraction of bytes the sort did not move (skipped passes) would mean nothing: null
         res["roofline_frac_plain_bytes"] = {
-            m: plain_bytes / (res[m + "_ms"] / 1e3) / 1e9 / peak for m in ("plain", "learned")}
+            m: (plain_bytes / (res[m + "_ms"] / 1e3) / 1e9 / peak if res["plain_passes_run"] == full_passes else None)
+            for m in ("plain", "learned")}
         st = res["learned_stats"]
         learned_bytes = (st["partition_passes"] + 1) * n * 2 * (kb + vb)
         res["roofline_frac_learned_bytes"] = learned_bytes / (res["learned_ms"] / 1e3) / 1e9 / peak
@@ -570,6 +604,9 @@ def run_engine(args):
     with ClockSampler(local) as clocks:
         ms = time_steps(torch, main.run, args.steps, args.warmup, barrier)
     ms, value = job_throughput(torch, ms, n, world, "cuda")
+    # the headline result itself: sorted by key, equal keys in index order, values a
+    # permutation of the indices naming their keys (checked on the GPU, outside the timing)
+    verified = check_sorted_pairs(main.ki, main.ko, main.vo, "u")
 
     # per-kernel durations (observer run, separate from the timed steps)
     ktimes, launches = kernel_times(torch, main, max(3, args.steps // 2))
@@ -709,13 +746,18 @@ def run_engine(args):
             else:
                 vms = time_steps(torch, s.run, max(3, args.steps // 2), 2, barrier)
             kt, _ = kernel_times(torch, s, 3)
+            run = passes_that_run(torch, kk, s.begin_bit, s.end_bit)
             variants.append({
                 "name": name,
                 "num_items": nv,
                 "keys_per_s": nv / (vms / 1000.0),
                 "ms": vms,
                 "passes": s.passes,
-                "roofline_frac": s.algorithmic_bytes() / (vms / 1000.0) / 1e9 / peak,
+                "passes_run": run,
+                # null where passes were skipped: those moved no bytes
+                "roofline_frac": (s.algorithmic_bytes() / (vms / 1000.0) / 1e9 / peak) if run == s.passes else None,
+                "verified": check_sorted_pairs(s.ki, s.ko, s.vo, "u", sp.get("descending", False))
+                if s.vo is not None and s.begin_bit == 0 and s.end_bit == 8 * s.key_bytes else None,
                 "onesweep_ms": kt.get("onesweep"),
                 "histogram_ms": kt.get("histogram"),
             })
@@ -765,6 +807,7 @@ def run_engine(args):
                 "single_step": {"value": n / (e2e_single_ms / 1000.0), "ms_per_step": e2e_single_ms,
                                 "mode": "one batch at a time: upload, sort, download"}},
         "cpu_baseline": cpu,
+        "verified": verified,
         "variants": variants,
         "segmented": segmented,
         "learned": learned,

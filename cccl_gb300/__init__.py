@@ -6,7 +6,7 @@ counterparts) call the library's C ABI. There is no CPU fallback: without the bu
 """
 
 from .build import build, library_path
-from .radix_sort import DoubleBuffer, SortOrder, make_radix_sort, radix_sort
+from .radix_sort import DoubleBuffer, SortOrder, make_radix_sort, radix_sort, sort_status
 from .segmented_sort import make_segmented_radix_sort, make_segmented_sort, segmented_radix_sort, segmented_sort
 from .learned_sort import learned_sort, make_learned_sort
 
@@ -17,6 +17,7 @@ __all__ = [
     "SortOrder",
     "make_radix_sort",
     "radix_sort",
+    "sort_status",
     "make_segmented_sort",
     "segmented_sort",
     "make_segmented_radix_sort",

@@ -195,7 +195,13 @@ EXPORTED_SYMBOLS = [
     "cccl_gb300_learned_sort_stats",
     "cccl_gb300_learned_sort_cleanup",
     "cccl_gb300_segmented_radix_sort",
+    "cccl_gb300_sort_status",
+    "cccl_gb300_testing_set_wait_fault",
 ]
+
+# CCCL_GB300_STATUS_* bits (include/cccl_gb300/sort_status.h)
+STATUS_WAIT_TIMEOUT, STATUS_BAD_SEGMENT, STATUS_SEG_CAPACITY = 1, 2, 4
+CUDA_ERROR_LAUNCH_TIMEOUT = 702
 
 NOALLOC_MAX_ITEMS = 1 << 20  # CCCL_GB300_NOALLOC_MAX_ITEMS
 
@@ -283,6 +289,8 @@ def _declare(lib):
         P(LearnedSortStats),
     ]
     lib.cccl_gb300_learned_sort_cleanup.argtypes = [L]
+    lib.cccl_gb300_sort_status.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, P(C.c_uint32)]
+    lib.cccl_gb300_testing_set_wait_fault.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64]
     for name in EXPORTED_SYMBOLS:
         if name not in ("cccl_serialization_buffer_free", "cccl_gb300_set_launch_observer"):
             getattr(lib, name).restype = C.c_int

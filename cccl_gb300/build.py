@@ -49,6 +49,7 @@ HOST_SOURCES = [
     "segmented_sort_abi.cpp",
     "learned_plan.cpp",
     "learned_sort_abi.cpp",
+    "status_abi.cpp",
 ]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]

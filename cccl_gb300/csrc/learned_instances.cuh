@@ -11,6 +11,18 @@ extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitPa
   gb300::init_body(p);
 }
 
+extern "C" __global__ void __launch_bounds__(32) gb300_status_fold(const gb300::StatusFoldParams p)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+  {
+    const uint32_t bits = __ldcg(p.src) & p.mask;
+    if (bits != 0u)
+    {
+      atomicOr(p.dst, bits);
+    }
+  }
+}
+
 #define GB300_LEARNED_PASS(KB, VB, FP, FS)                                                                        \
   static_assert(gb300::PersistentSmem<KB, VB, gb300::persistent_tpb(KB, VB), gb300::learned_items(KB, VB),        \
                                       gb300::learned_extra_bytes(KB, VB, gb300::learned_items(KB, VB))>::bytes    \

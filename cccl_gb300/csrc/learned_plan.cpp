@@ -237,6 +237,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     size_t bytes          = t.sample_temp_bytes;
     sc.temp_storage_bytes = &bytes;
     sc.stream             = c.stream;
+    sc.status_word        = &ctrl->status;
     radix_sort_dispatch(s.sample_pol, s.sample_ks, sc, &ssel);
   }
   {
@@ -409,6 +410,14 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     sc.temp_storage_bytes = &bytes;
     int seg_sel           = 0;
     segmented_sort_dispatch(s.seg_pol, s.seg_ks, sc, &seg_sel);
+    // its errors are the call's; a bucket too large for it is not (step 9 sorts it)
+    {
+      StatusFoldParams fp{};
+      fp.dst  = &ctrl->status;
+      fp.src  = reinterpret_cast<const uint32_t*>(base + t.seg_off) + SEG_CTR_STATUS;
+      fp.mask = ~STATUS_BAD_SEGMENT;
+      launch("learned_status", s.lk.status_fold, 1, 32, 0, c.stream, fp);
+    }
     // 9. a bucket of 2^30 or more keys was left unsorted: a stable sort of the partitioned
     // keys equals the stable sort of the input (the partition keeps equal keys in order),
     // so the plain radix sort of them into the final buffer finishes the job
@@ -430,6 +439,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
       fc.stream             = c.stream;
       fc.gate.gate          = reinterpret_cast<const uint32_t*>(base + t.seg_off) + SEG_CTR_STATUS;
       fc.gate.gate_mask     = STATUS_BAD_SEGMENT;
+      fc.status_word        = &ctrl->status;
       int fsel              = 0;
       radix_sort_dispatch(s.plain_pol, s.plain_ks, fc, &fsel);
     }
@@ -452,6 +462,7 @@ void learned_sort_dispatch(const LearnedSetup& s, const RadixCall& c, int* selec
     pc.temp_storage_bytes = &pbytes;
     pc.stream             = c.stream;
     pc.gate               = plain_gate;
+    pc.status_word        = &ctrl->status;
     int psel              = 0;
     radix_sort_dispatch(s.plain_pol, s.plain_ks, pc, &psel);
   }

@@ -29,6 +29,7 @@ struct LearnedKernels
   CUkernel bounds;
   CUkernel bucket4k; // bucket sort, up to 4096 keys per bucket
   CUkernel bucket8k; // up to 8192
+  CUkernel status_fold; // a sub-sort's error bits into the call's status word
 };
 
 // Everything one (key type, value width, order) needs; lives in the build result.

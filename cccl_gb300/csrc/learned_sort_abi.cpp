@@ -184,6 +184,7 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
     const std::string k  = std::to_string(kb);
     const std::string fs = kind == KIND_FLOAT ? "f" : "i";
     s->lk.init   = get_kernel(r.learned_library, "gb300_init");
+    s->lk.status_fold = get_kernel(r.learned_library, "gb300_status_fold");
     s->lk.sample = get_kernel(r.learned_library, "gb300_learned_sample_k" + k + "_" + fs);
     s->lk.fit    = get_kernel(r.learned_library, "gb300_learned_fit_k" + k);
     s->lk.cells  = get_kernel(r.learned_library, "gb300_learned_cells_k" + k);

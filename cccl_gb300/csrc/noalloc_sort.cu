@@ -4,8 +4,11 @@
 //
 // The kernels are the plain path's (init, all-pass histogram, CTA-per-tile onesweep pass,
 // single tile), instantiated here so the runtime API can launch them next to the array.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <mutex>
 
@@ -21,7 +24,9 @@ using namespace gb300;
 constexpr int KB                = 4;
 constexpr uint32_t MAX_ITEMS    = CCCL_GB300_NOALLOC_MAX_ITEMS;
 constexpr int MAX_SORT_PASSES   = 4; // 32-bit keys
-constexpr int TILE_MIN          = ONESWEEP_TPB * 16; // smallest tile of the two variants (pairs)
+// smallest tile of the two pass kernels below (keys only, pairs): it sizes the look-back rows
+constexpr int TILE_MIN          = ONESWEEP_TPB * std::min(onesweep_items(KB, 0), onesweep_items(KB, 4));
+static_assert(TILE_MIN >= ONESWEEP_TPB, "a pass tile holds at least one key per thread");
 constexpr uint32_t MAX_TILES    = (MAX_ITEMS + TILE_MIN - 1) / TILE_MIN;
 constexpr size_t CTRL_BYTES     = (sizeof(SortControl) + 4 * MAX_SORT_PASSES + 255) / 256 * 256;
 constexpr size_t BINS_BYTES     = 8 * 256 * MAX_SORT_PASSES;
@@ -29,6 +34,10 @@ constexpr size_t LOOKBACK_WORDS = size_t(MAX_TILES) * 256;
 constexpr size_t LOOKBACK_BYTES = 2 * 4 * LOOKBACK_WORDS;
 constexpr size_t TMP_BYTES      = size_t(MAX_ITEMS) * 4;
 constexpr size_t SCRATCH_BYTES  = CTRL_BYTES + BINS_BYTES + LOOKBACK_BYTES + 2 * TMP_BYTES;
+// The size the header documents (8,763,648 bytes = 8.36 MiB); a change of the tile table
+// that moves it must move the documentation with it.
+static_assert(SCRATCH_BYTES == CCCL_GB300_NOALLOC_SCRATCH_BYTES, "documented scratch size");
+static_assert(offsetof(SortControl, status) == 0, "the status word is word 0 of the scratch array");
 
 // The scratch space. In host code this name is only a stand-in for the symbol: the device
 // address comes from cudaGetSymbolAddress (scratch_on_current_device below).
@@ -59,50 +68,90 @@ __global__ void __launch_bounds__(SINGLE_TILE_TPB) na_single_tile_pairs(const Si
   single_tile_body<KB, 4, false, SINGLE_TILE_TPB, SINGLE_TILE_ITEMS>(p);
 }
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[MAX_DEVICES] = {};
-
-// Once per device, with that device current: the array's device address and the
-// shared-memory attributes of the kernels that need more than 48 KB.
-cudaError_t scratch_on_current_device(unsigned char** out)
+// Set-up, once per CUDA context (in the usual case, the runtime's primary context of each
+// device, so once per device): with that context current, the array's device address from
+// cudaGetSymbolAddress, and the shared-memory attributes of the kernels that need more than
+// 48 KB. It is keyed on the context's unique id, not on the device number, so a caller that
+// makes another context current, or a context created after cudaDeviceReset, gets that
+// context's own copy of the array and never a stale address.
+constexpr int MAX_CONTEXTS = 64;
+struct ContextScratch
 {
-  int dev = 0;
-  if (cudaError_t e = cudaGetDevice(&dev); e != cudaSuccess)
+  unsigned long long ctx_id;
+  unsigned char* ptr;
+};
+std::mutex g_setup_mutex;
+ContextScratch g_scratch[MAX_CONTEXTS] = {};
+int g_scratch_used                     = 0;
+
+cudaError_t setup_current_context(unsigned char** out)
+{
+  void* ptr = nullptr;
+  if (cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch); e != cudaSuccess)
   {
     return e;
   }
-  if (dev < 0 || dev >= MAX_DEVICES)
+  const struct
   {
-    return cudaErrorInvalidDevice;
-  }
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (g_scratch_ptr[dev] == nullptr)
+    const void* fn;
+    size_t smem;
+  } attrs[] = {{(const void*) na_onesweep_keys, onesweep_smem_bytes(KB, 0)},
+               {(const void*) na_onesweep_pairs, onesweep_smem_bytes(KB, 4)},
+               {(const void*) na_single_tile_keys, single_tile_smem_bytes(KB)},
+               {(const void*) na_single_tile_pairs, single_tile_smem_bytes(KB)}};
+  for (const auto& a : attrs)
   {
-    void* ptr = nullptr;
-    if (cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch); e != cudaSuccess)
+    if (cudaError_t e = cudaFuncSetAttribute(a.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(a.smem));
+        e != cudaSuccess)
     {
       return e;
     }
-    const struct
-    {
-      const void* fn;
-      size_t smem;
-    } attrs[] = {{(const void*) na_onesweep_keys, onesweep_smem_bytes(KB, 0)},
-                 {(const void*) na_onesweep_pairs, onesweep_smem_bytes(KB, 4)},
-                 {(const void*) na_single_tile_keys, single_tile_smem_bytes(KB)},
-                 {(const void*) na_single_tile_pairs, single_tile_smem_bytes(KB)}};
-    for (const auto& a : attrs)
-    {
-      if (cudaError_t e = cudaFuncSetAttribute(a.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(a.smem));
-          e != cudaSuccess)
-      {
-        return e;
-      }
-    }
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(ptr);
   }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<unsigned char*>(ptr);
+  return cudaSuccess;
+}
+
+cudaError_t scratch_on_current_context(unsigned char** out)
+{
+  CUcontext ctx = nullptr;
+  if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS)
+  {
+    return cudaErrorInitializationError;
+  }
+  if (ctx == nullptr)
+  {
+    // no context yet: the runtime binds the current device's primary context on this call
+    if (cudaError_t e = setup_current_context(out); e != cudaSuccess)
+    {
+      return e;
+    }
+    if (cuCtxGetCurrent(&ctx) != CUDA_SUCCESS || ctx == nullptr)
+    {
+      return cudaErrorInitializationError;
+    }
+  }
+  unsigned long long id = 0;
+  if (cuCtxGetId(ctx, &id) != CUDA_SUCCESS)
+  {
+    return cudaErrorInitializationError;
+  }
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  for (int i = 0; i < g_scratch_used; ++i)
+  {
+    if (g_scratch[i].ctx_id == id)
+    {
+      *out = g_scratch[i].ptr;
+      return cudaSuccess;
+    }
+  }
+  if (cudaError_t e = setup_current_context(out); e != cudaSuccess)
+  {
+    return e;
+  }
+  if (g_scratch_used < MAX_CONTEXTS) // beyond that, every call repeats the set-up (still correct)
+  {
+    g_scratch[g_scratch_used++] = ContextScratch{id, *out};
+  }
   return cudaSuccess;
 }
 
@@ -141,22 +190,37 @@ extern "C" CCCL_GB300_API CUresult cccl_gb300_radix_sort_u32_noalloc(
                 MAX_ITEMS);
     return CUDA_ERROR_INVALID_VALUE;
   }
-  if (begin_bit < 0 || end_bit > 32 || begin_bit > end_bit || d_keys_in == nullptr || d_keys_out == nullptr
-      || ((d_values_in == nullptr) != (d_values_out == nullptr)))
+  if (begin_bit < 0 || end_bit > 32 || begin_bit > end_bit
+      || (num_items > 0
+          && (d_keys_in == nullptr || d_keys_out == nullptr || ((d_values_in == nullptr) != (d_values_out == nullptr)))))
   {
     std::printf("\nERROR in cccl_gb300_radix_sort_u32_noalloc(): invalid arguments\n");
     return CUDA_ERROR_INVALID_VALUE;
   }
   unsigned char* scratch = nullptr;
-  if (cudaError_t e = scratch_on_current_device(&scratch); e != cudaSuccess)
+  if (cudaError_t e = scratch_on_current_context(&scratch); e != cudaSuccess)
   {
     return fail("setup", e);
+  }
+  cudaStream_t stream = reinterpret_cast<cudaStream_t>(stream_handle);
+  auto* ctrl          = reinterpret_cast<SortControl*>(scratch);
+  // launches are checked one at a time, so an error names the kernel that failed
+  auto launched = [](const char* kernel) {
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? CUDA_SUCCESS : fail(kernel, e);
+  };
+  if (num_items == 0 || begin_bit == end_bit || num_items <= cub_single_tile_limit(KB, d_values_in ? 4 : 0))
+  {
+    // these paths wait on nothing: the status word must still read "no error" afterwards
+    if (cudaError_t e = cudaMemsetAsync(&ctrl->status, 0, sizeof(uint32_t), stream); e != cudaSuccess)
+    {
+      return fail("status reset", e);
+    }
   }
   if (num_items == 0)
   {
     return CUDA_SUCCESS;
   }
-  cudaStream_t stream   = reinterpret_cast<cudaStream_t>(stream_handle);
   const bool pairs      = d_values_in != nullptr;
   const uint64_t n      = num_items;
   const KeyCodec codec  = unsigned_codec(descending);
@@ -183,20 +247,16 @@ extern "C" CCCL_GB300_API CUresult cccl_gb300_radix_sort_u32_noalloc(
     if (pairs)
     {
       na_single_tile_pairs<<<1, SINGLE_TILE_TPB, single_tile_smem_bytes(KB), stream>>>(p);
+      return launched("launch of the single-tile pairs kernel");
     }
-    else
-    {
-      na_single_tile_keys<<<1, SINGLE_TILE_TPB, single_tile_smem_bytes(KB), stream>>>(p);
-    }
-    const cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? CUDA_SUCCESS : fail("launch", e);
+    na_single_tile_keys<<<1, SINGLE_TILE_TPB, single_tile_smem_bytes(KB), stream>>>(p);
+    return launched("launch of the single-tile keys kernel");
   }
 
   const int passes    = (end_bit - begin_bit + RADIX_BITS - 1) / RADIX_BITS;
   const uint64_t tile = uint64_t(ONESWEEP_TPB) * onesweep_items(KB, pairs ? 4 : 0);
   const uint32_t tiles = uint32_t((n + tile - 1) / tile);
 
-  auto* ctrl      = reinterpret_cast<SortControl*>(scratch);
   auto* tile_ctrs = reinterpret_cast<uint32_t*>(scratch + sizeof(SortControl));
   auto* bins      = reinterpret_cast<unsigned long long*>(scratch + CTRL_BYTES);
   uint32_t* lb[2] = {reinterpret_cast<uint32_t*>(scratch + CTRL_BYTES + BINS_BYTES),
@@ -207,8 +267,12 @@ extern "C" CCCL_GB300_API CUresult cccl_gb300_radix_sort_u32_noalloc(
   {
     InitParams p{};
     p.words     = reinterpret_cast<uint32_t*>(ctrl);
-    p.num_words = CTRL_BYTES / 4; // counters restart from zero on every call
+    p.num_words = CTRL_BYTES / 4; // counters and the status word restart from zero on every call
     na_init<<<unsigned((p.num_words + 255) / 256), 256, 0, stream>>>(p);
+    if (const CUresult r = launched("launch of the init kernel"); r != CUDA_SUCCESS)
+    {
+      return r;
+    }
   }
   {
     HistogramParams p{};
@@ -225,6 +289,10 @@ extern "C" CCCL_GB300_API CUresult cccl_gb300_radix_sort_u32_noalloc(
     p.lookback_words = size_t(tiles) * 256;
     const unsigned grid = unsigned(std::min<uint64_t>(512, (n + HISTOGRAM_TPB * 4 - 1) / (HISTOGRAM_TPB * 4)));
     na_histogram<<<grid, HISTOGRAM_TPB, 0, stream>>>(p);
+    if (const CUresult r = launched("launch of the histogram kernel"); r != CUDA_SUCCESS)
+    {
+      return r;
+    }
   }
   const void* ksrc = d_keys_in;
   const void* vsrc = d_values_in;
@@ -263,9 +331,26 @@ extern "C" CCCL_GB300_API CUresult cccl_gb300_radix_sort_u32_noalloc(
     {
       na_onesweep_keys<<<tiles, ONESWEEP_TPB, onesweep_smem_bytes(KB, 0), stream>>>(op);
     }
+    if (const CUresult r = launched(pairs ? "launch of the pairs digit pass" : "launch of the keys digit pass");
+        r != CUDA_SUCCESS)
+    {
+      return r;
+    }
     ksrc = kdst;
     vsrc = vdst;
   }
-  const cudaError_t e = cudaGetLastError();
-  return e == cudaSuccess ? CUDA_SUCCESS : fail("launch", e);
+  return CUDA_SUCCESS;
+}
+
+// The status word of the allocation-free entry point in the current context, for
+// cccl_gb300_sort_status (status_abi.cpp). Returns 0 or a cudaError_t.
+int gb300_noalloc_status_word(uint32_t** dptr)
+{
+  unsigned char* scratch = nullptr;
+  if (cudaError_t e = scratch_on_current_context(&scratch); e != cudaSuccess)
+  {
+    return int(e);
+  }
+  *dptr = &reinterpret_cast<SortControl*>(scratch)->status;
+  return 0;
 }

@@ -50,13 +50,6 @@ struct OnesweepSmem
 // CTA, [3] single-digit tile flag and digit, [8..15] scan scratch, [16..19] two mbarriers
 // (persistent kernel).
 
-// Compile-time flag carried by a value (for generic lambdas).
-template <bool B>
-struct BoolTag
-{
-  static constexpr bool value = B;
-};
-
 // Where a pass takes its digits from.
 //   RadixDigits: bits [current_bit, current_bit + num_bits) of the encoded key, recomputed
 //     wherever needed (histogram, ranking, write-out);
@@ -271,7 +264,11 @@ __device__ __forceinline__ void onesweep_tile(
       named_barrier_256();
     }
     uint32_t* lb_row     = p.lookback + (size_t) (p.tile_row_base + tile) * R;
-    store_status(lb_row + tid, (tile == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+    const bool publish   = tile != gb300_fault_skip_tile; // always, unless a test withholds this tile
+    if (publish)
+    {
+      store_status(lb_row + tid, (tile == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+    }
     asm volatile("bar.arrive 2, %0;" ::"n"(TPB) : "memory");
 
     uint32_t excl = 0;
@@ -279,7 +276,10 @@ __device__ __forceinline__ void onesweep_tile(
     if (tile > 0)
     {
       excl = lookback_walk(p, tile, tid, failed);
-      store_status(lb_row + tid, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+      if (publish)
+      {
+        store_status(lb_row + tid, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+      }
       if (failed)
       {
         atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);
@@ -651,6 +651,12 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
   constexpr int TILE = L::TILE;
   static_assert(STABLE || VB == 0, "pairs need a stable pass");
   static_assert(STABLE || !Digits::computed, "computed digits are ranked stably");
+  // peers by lane-mask tables (GB300_RANK_MODE 1, or 2 for every other item) where the tables
+  // of all main warps fit in one tile buffer
+#ifndef GB300_RANK_MODE
+#  define GB300_RANK_MODE 0
+#endif
+  constexpr bool RANK_TABLE = GB300_RANK_MODE != 0 && size_t(NW) * R * 4 <= L::buf_bytes;
 
   extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
@@ -979,6 +985,20 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
         {
           warp_rank_stable_digits<ITEMS>(dg.d, pos, whist + warp * R);
         }
+        else if constexpr (STABLE && RANK_TABLE)
+        {
+          // the warp's lane-mask table lives in this tile's own buffer: every main thread
+          // read its keys (and values) from it before BO, and nothing is staged into it
+          // before the main barrier below
+          uint32_t* tbl = reinterpret_cast<uint32_t*>(smem + L::buf_off + size_t(buf) * L::buf_bytes) + warp * R;
+#pragma unroll
+          for (int k = lane; k < R; k += 32)
+          {
+            tbl[k] = 0u;
+          }
+          __syncwarp();
+          warp_rank_stable_table<U, FP, ITEMS, GB300_RANK_MODE == 2>(keys, pos, whist + warp * R, tbl, bit, dmask);
+        }
         else if constexpr (STABLE)
         {
           warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
@@ -987,6 +1007,10 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
         {
           warp_rank_unstable_tail<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask, wofs, valid);
         }
+      }
+      if constexpr (STABLE && RANK_TABLE && !Digits::computed)
+      {
+        asm volatile("bar.sync 6, %0;" ::"n"(MT) : "memory"); // every warp has ranked: the tables are dead
       }
       U* ks = kbuf(buf);
 #pragma unroll
@@ -1033,7 +1057,8 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
   else
   {
     // ============================== look-back threads ==============================
-    const int d = tid - MT; // this thread's digit
+    const int d                = tid - MT; // this thread's digit
+    const uint32_t skip_tile   = gb300_fault_skip_tile; // no tile, unless a test withholds one
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
     {
       const uint32_t valid = min(uint32_t(TILE), p.portion_items - t * TILE);
@@ -1048,8 +1073,12 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
         const uint32_t real      = total - (uint32_t(d) == pad_digit ? uint32_t(TILE) - valid : 0u);
         misc[3]                  = real == valid ? (1u | (uint32_t(d) << 8)) : 0u;
       }
-      uint32_t* lb_row = p.lookback + (size_t) (p.tile_row_base + t) * R;
-      store_status(lb_row + d, (t == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+      uint32_t* lb_row   = p.lookback + (size_t) (p.tile_row_base + t) * R;
+      const bool publish = t != skip_tile;
+      if (publish)
+      {
+        store_status(lb_row + d, (t == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+      }
       asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO
 
       uint32_t excl = 0;
@@ -1057,7 +1086,10 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
       {
         bool failed = false;
         excl        = lookback_walk<PERSISTENT_LOOKBACK_BATCH>(p, t, d, failed);
-        store_status(lb_row + d, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+        if (publish)
+        {
+          store_status(lb_row + d, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+        }
         if (failed)
         {
           atomicOr(p.status, STATUS_LOOKBACK_TIMEOUT);

@@ -49,10 +49,10 @@
   }
 
 #define GB300_HISTOGRAM(KB, FP, SUF)                                                                              \
-  extern "C" __global__ void __launch_bounds__(gb300::HISTOGRAM_TPB, gb300::HISTOGRAM_MINB)                     \
+  extern "C" __global__ void __launch_bounds__(gb300::HISTOGRAM_LANES_TPB, 1)                                   \
     gb300_histogram_k##KB##_##SUF(const gb300::HistogramParams p)                                               \
   {                                                                                                             \
-    gb300::histogram_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                                     \
+    gb300::histogram_lanes_body<KB, FP, gb300::HISTOGRAM_LANES_TPB>(p);                                         \
   }
 
 // Single-tile kernels of descending floating-point sorts: CUB's single tile folds -0.0 into

@@ -241,6 +241,162 @@ __device__ __forceinline__ void histogram_body(const HistogramParams& p)
 }
 
 // ---------------------------------------------------------------------------------------
+// Lane-column histogram: the all-pass digit counts of the plain sort, one CTA per SM.
+//
+// The reference counts into one shared table per CTA with an atomic per digit
+// (cub/cub/agent/agent_radix_sort_histogram.cuh:96-285); on GB300 that is bound by bank
+// conflicts among the 32 random addresses of each warp-wide atomic (measured: ~0.4 of HBM).
+// Here the counter of (pass q, digit d) for lane l is its own word, laid out so that the 32
+// lanes of a warp always hit 32 different banks:
+//   byte offset = block(q) << 16 | d << 8 | byte0(q, l)
+//   q < 4:  block = q >> 1, byte0 = (q & 1) * 128 + l * 4        (32 columns)
+//   q >= 4: block = 2,      byte0 = (q & 3) * 64 + (l & 15) * 4  (16 columns, lanes l, l+16 share)
+// so one byte permute (digit byte q of the key into byte 1 of a per-lane constant) gives the
+// counter's address, and one reduction-add (no return value) counts the key: two
+// instructions per key and pass. Every CTA of the kernel shares the columns among its warps
+// (the adds are atomic). At the end each row of columns is summed by a warp and the totals go
+// to histogram_finish. Keys are streamed with four 16-byte loads in flight per thread.
+// ---------------------------------------------------------------------------------------
+template <int KB, int FP, int TPB>
+__device__ __forceinline__ void histogram_lanes_body(const HistogramParams& p)
+{
+  using U           = typename uint_of<KB>::type;
+  constexpr int R   = RADIX_DIGITS;
+  constexpr int QN  = KB;          // passes of a whole key
+  constexpr int VEC = 16 / KB;     // keys per 16-byte load
+  extern __shared__ __align__(16) unsigned char table[];
+  __shared__ uint32_t sh[MAX_PASSES * R];
+  if (!gate_open(p.gate))
+  {
+    return;
+  }
+  const int tid  = threadIdx.x;
+  const int lane = tid & 31;
+  const int P    = p.num_passes;
+  const uint32_t table_bytes = uint32_t(histogram_table_bytes(P));
+  for (uint32_t i = uint32_t(tid) * 16u; i < table_bytes; i += uint32_t(TPB) * 16u)
+  {
+    *reinterpret_cast<uint4*>(table + i) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  uint32_t col[QN]; // byte 0 and byte 2 of every pass's counter offsets for this lane
+#pragma unroll
+  for (int q = 0; q < QN; ++q)
+  {
+    col[q] = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(q & 1) * 128u + uint32_t(lane) * 4u))
+                   : ((2u << 16) | (uint32_t(q & 3) * 64u + uint32_t(lane & 15) * 4u));
+  }
+  __syncthreads();
+
+  const int bb        = p.begin_bit;
+  const int wbits     = p.end_bit - p.begin_bit;
+  const U wmask       = wbits >= 8 * KB ? U(~U(0)) : U((U(1) << wbits) - U(1));
+  const bool windowed = bb != 0 || wbits != 8 * KB;
+  auto count_key = [&](U raw, auto window_tag) {
+    U t = digit_source<U, FP>(encode_key<U>(raw, p.codec));
+    if constexpr (decltype(window_tag)::value)
+    {
+      t = U(U(t >> bb) & wmask);
+    }
+    const uint32_t lo = uint32_t(t);
+    uint32_t hi       = 0;
+    if constexpr (KB == 8)
+    {
+      hi = uint32_t((unsigned long long) t >> 32);
+    }
+#pragma unroll
+    for (int q = 0; q < QN; ++q)
+    {
+      if (q < P)
+      {
+        // byte 0 and byte 2 from the lane's column word, byte 1 = digit q, byte 3 = 0
+        const uint32_t off = __byte_perm(q < 4 ? lo : hi, col[q], 0x7604u | (uint32_t(q & 3) << 4));
+        atomicAdd(reinterpret_cast<uint32_t*>(table + off), 1u);
+      }
+    }
+  };
+  auto count_all = [&](auto window_tag) {
+    const U* keys                 = static_cast<const U*>(p.keys);
+    const unsigned long long n    = p.num_items;
+    const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
+    unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
+    if (head > n)
+    {
+      head = n;
+    }
+    const unsigned long long nvec     = (n - head) / VEC;
+    const unsigned long long body_end = head + nvec * VEC;
+    if (blockIdx.x == 0)
+    {
+      for (unsigned long long i = tid; i < head; i += TPB)
+      {
+        count_key(keys[i], window_tag);
+      }
+      for (unsigned long long i = body_end + tid; i < n; i += TPB)
+      {
+        count_key(keys[i], window_tag);
+      }
+    }
+    const uint4* vkeys                = reinterpret_cast<const uint4*>(keys + head);
+    const unsigned long long stride   = (unsigned long long) gridDim.x * TPB;
+    unsigned long long v              = blockIdx.x * (unsigned long long) TPB + tid;
+    auto count_vec = [&](const uint4& w) {
+      U k[VEC];
+      memcpy(k, &w, 16);
+#pragma unroll
+      for (int j = 0; j < VEC; ++j)
+      {
+        count_key(k[j], window_tag);
+      }
+    };
+    for (; v + 3 * stride < nvec; v += 4 * stride)
+    {
+      uint4 w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        w[j] = __ldcs(vkeys + v + j * stride);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        count_vec(w[j]);
+      }
+    }
+    for (; v < nvec; v += stride)
+    {
+      count_vec(__ldcs(vkeys + v));
+    }
+  };
+  if (windowed)
+  {
+    count_all(BoolTag<true>{});
+  }
+  else
+  {
+    count_all(BoolTag<false>{});
+  }
+  __syncthreads();
+
+  // one warp per row of columns: the CTA's count of (pass, digit)
+  const int warp = tid >> 5;
+  for (int r = warp; r < P * R; r += TPB / 32)
+  {
+    const int q          = r >> 8;
+    const int d          = r & (R - 1);
+    const int width      = q < 4 ? 32 : 16;
+    const uint32_t base  = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(d) << 8) | (uint32_t(q & 1) * 128u))
+                                 : ((2u << 16) | (uint32_t(d) << 8) | (uint32_t(q & 3) * 64u));
+    const uint32_t x     = lane < width ? *reinterpret_cast<const uint32_t*>(table + base + 4u * uint32_t(lane)) : 0u;
+    const uint32_t total = __reduce_add_sync(0xffffffffu, x);
+    if (lane == 0)
+    {
+      sh[r] = total;
+    }
+  }
+  histogram_finish<TPB>(p, sh);
+}
+
+// ---------------------------------------------------------------------------------------
 // single tile: the whole LSD sort of <= TPB*ITEMS keys inside one CTA
 // ---------------------------------------------------------------------------------------
 template <int KB, int TPB, int ITEMS>

@@ -27,7 +27,7 @@ RadixPolicy make_radix_policy(int key_bytes, int value_bytes, int key_kind)
   p.onesweep_items    = onesweep_items(key_bytes, value_bytes);
   p.single_tile_tpb   = SINGLE_TILE_TPB;
   p.single_tile_items = SINGLE_TILE_ITEMS;
-  p.histogram_tpb     = HISTOGRAM_TPB;
+  p.histogram_tpb     = HISTOGRAM_LANES_TPB;
   p.onesweep_smem     = onesweep_smem_bytes(key_bytes, value_bytes);
   p.persistent_tpb    = persistent_tpb(key_bytes, value_bytes);
   p.persistent_items  = persistent_items(key_bytes, value_bytes);
@@ -101,6 +101,17 @@ static bool aligned16(const void* p)
   return (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
 }
 
+// Paths that use no temporary storage still leave word 0 of a caller's buffer (the status
+// word the onesweep path reports into) reading "no error", so that a status query after any
+// call reads that call's status, not an earlier one's.
+static void clear_status_word(const RadixCall& c)
+{
+  if (c.status_word == nullptr && c.d_temp_storage != nullptr && *c.temp_storage_bytes >= 4)
+  {
+    check(cuMemsetD32Async(CUdeviceptr(c.d_temp_storage), 0u, 1, c.stream), "cuMemsetD32Async(status)");
+  }
+}
+
 static void check_aligned(const void* p, size_t a, const char* what)
 {
   if (p != nullptr && (reinterpret_cast<uintptr_t>(p) % a) != 0)
@@ -137,6 +148,10 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     {
       *c.temp_storage_bytes = 1;
     }
+    else
+    {
+      clear_status_word(c);
+    }
     return;
   }
   for (int i = 0; i < 2; ++i)
@@ -165,6 +180,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       *c.temp_storage_bytes = 1;
       return;
     }
+    clear_status_word(c);
     check(cuMemcpyAsync(CUdeviceptr(c.keys[1]), CUdeviceptr(c.keys[0]), n * kb, c.stream), "cuMemcpyAsync(keys)");
     if (has_vals)
     {
@@ -191,6 +207,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     p.begin_bit  = c.begin_bit;
     p.end_bit    = c.end_bit;
     p.codec      = codec;
+    clear_status_word(c);
     launch("single_tile", ks.single_tile, 1, unsigned(pol.single_tile_tpb), pol.single_tile_smem, c.stream, p);
     *selector = 1;
     return;
@@ -250,9 +267,10 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
     // the pass plan: passes whose digit is the same for every key are skipped
     p.plan      = ctrl->plan;
     p.plan_mode = c.overwrite ? PLAN_MODE_DOUBLE : PLAN_MODE_SEPARATE;
-    const uint64_t want = ceil_div(n, uint64_t(pol.histogram_tpb) * (16 / kb) * 4);
-    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sm_count()) * 4)));
-    launch("histogram", ks.histogram, grid, unsigned(pol.histogram_tpb), 0, c.stream, p);
+    // one lane-column CTA per SM (fewer for small inputs: four 16-byte loads per thread)
+    const uint64_t want = ceil_div(n, uint64_t(HISTOGRAM_LANES_TPB) * (16 / kb) * 4);
+    const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(want, uint64_t(sm_count()))));
+    launch("histogram", ks.histogram, grid, unsigned(HISTOGRAM_LANES_TPB), histogram_table_bytes(passes), c.stream, p);
   }
   // 3. one onesweep launch per (pass, portion)
   void* kdst[MAX_PASSES];
@@ -305,7 +323,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.tile_counter  = tile_ctrs + (size_t(p) * t.num_portions + q);
       op.bins          = bins + (size_t(p) * t.num_portions + q) * RADIX_DIGITS;
       op.bins_next     = (q + 1 < t.num_portions) ? bins + (size_t(p) * t.num_portions + q + 1) * RADIX_DIGITS : nullptr;
-      op.status        = &ctrl->status;
+      op.status        = c.status_word != nullptr ? c.status_word : &ctrl->status;
       op.codec         = codec;
       op.current_bit   = bit;
       op.num_bits      = std::min(RADIX_BITS, c.end_bit - bit);

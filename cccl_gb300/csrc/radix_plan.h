@@ -66,6 +66,8 @@ struct RadixCall
   size_t* temp_storage_bytes;
   CUstream stream;
   KernelGate gate; // null: always run; else the kernels run only if the flag is set (onesweep path only)
+  uint32_t* status_word; // null: the call's own status word (word 0 of its temp storage); else
+                         // where its kernels report (a sort run inside another reports there)
 };
 
 // Byte layout of the temporary storage of one call.

@@ -186,6 +186,11 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   }
   if (n == 0 || nseg == 0)
   {
+    // nothing runs: word 0 (the status word) still reads "no error" for a status query
+    if (*c.temp_storage_bytes >= 4)
+    {
+      check(cuMemsetD32Async(CUdeviceptr(c.d_temp_storage), 0u, 1, c.stream), "cuMemsetD32Async(status)");
+    }
     return;
   }
   if (*c.temp_storage_bytes < total)

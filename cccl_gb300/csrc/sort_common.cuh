@@ -14,8 +14,24 @@
 
 #include "sort_params.h"
 
+// Test hooks of the bounded waits, one copy per kernel image. With the defaults they change
+// nothing. A test (cccl_gb300_testing_set_wait_fault) may name one tile of every digit pass
+// whose look-back counts are then never published, and shorten the wait limit, so that the
+// successors' waits run out, the pass reports STATUS_LOOKBACK_TIMEOUT and its kernels still
+// return (no GPU hang: every wait below gives up after gb300_wait_limit_ns). Global-namespace
+// variables keep their plain names as symbols, which is how the host finds them.
+__device__ uint32_t gb300_fault_skip_tile = 0xffffffffu;
+__device__ unsigned long long gb300_wait_limit_ns = gb300::LOOKBACK_TIMEOUT_NS;
+
 namespace gb300
 {
+
+// Compile-time flag carried by a value (for generic lambdas).
+template <bool B>
+struct BoolTag
+{
+  static constexpr bool value = B;
+};
 
 template <int BYTES>
 struct uint_of;
@@ -154,8 +170,8 @@ __device__ __forceinline__ void store_status(uint32_t* p, uint32_t v)
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Waits until the status word is non-empty. Gives up after LOOKBACK_TIMEOUT_NS and
-// returns LB_ERROR, so a stuck predecessor can never hang the GPU.
+// Waits until the status word is non-empty. Gives up after gb300_wait_limit_ns (1 s unless a
+// test shortened it) and returns LB_ERROR, so a stuck predecessor can never hang the GPU.
 __device__ __forceinline__ uint32_t wait_status(const uint32_t* p)
 {
   uint32_t v = load_status(p);
@@ -175,7 +191,7 @@ __device__ __forceinline__ uint32_t wait_status(const uint32_t* p)
     if (++spins > 32)
     {
       __nanosleep(64);
-      if (global_timer_ns() - start > LOOKBACK_TIMEOUT_NS)
+      if (global_timer_ns() - start > gb300_wait_limit_ns)
       {
         return LB_ERROR;
       }
@@ -249,7 +265,7 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 }
 
 // Waits for the barrier phase with the given parity to complete; gives up after
-// LOOKBACK_TIMEOUT_NS and returns false.
+// gb300_wait_limit_ns and returns false.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {
   if (mbar_try_wait(bar, parity))
@@ -259,7 +275,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
   const uint64_t start = global_timer_ns();
   while (!mbar_try_wait(bar, parity))
   {
-    if (global_timer_ns() - start > LOOKBACK_TIMEOUT_NS)
+    if (global_timer_ns() - start > gb300_wait_limit_ns)
     {
       return false;
     }

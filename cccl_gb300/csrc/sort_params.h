@@ -11,7 +11,7 @@ namespace gb300
 constexpr int RADIX_BITS    = 8;
 constexpr int RADIX_DIGITS  = 1 << RADIX_BITS;
 constexpr int MAX_PASSES    = 8; // 64-bit keys
-constexpr uint64_t LOOKBACK_TIMEOUT_NS = 1000000000ull; // 1 s
+constexpr uint64_t LOOKBACK_TIMEOUT_NS = 1000000000ull; // 1 s: the limit of every bounded wait
 constexpr int LOOKBACK_BATCH = 8; // predecessor rows read per look-back step
 
 // Status word bits reported by the kernels (OR-ed into SortControl::status).
@@ -29,16 +29,21 @@ struct KeyCodec
   unsigned long long inv_clr;
 };
 
-// Per-call control block at the start of temp storage; zeroed by the init kernel.
+// Per-call control block at the start of temp storage; zeroed by the init kernel. The
+// status word comes first: word 0 of every sort's temporary storage is its status word
+// (read by cccl_gb300_sort_status).
 struct SortControl
 {
-  unsigned long long counts[MAX_PASSES * RADIX_DIGITS]; // all-pass digit histogram
-  uint32_t hist_done;                                   // CTAs finished in the histogram
   uint32_t status;                                      // STATUS_* bits
+  uint32_t hist_done;                                   // CTAs finished in the histogram
   uint32_t pad[2];
+  unsigned long long counts[MAX_PASSES * RADIX_DIGITS]; // all-pass digit histogram
   uint32_t plan[MAX_PASSES];                            // PLAN_* word of every digit pass
   // followed by tile counters, one per (pass, portion)
 };
+static_assert(sizeof(uint32_t) * 4 + sizeof(unsigned long long) * MAX_PASSES * RADIX_DIGITS
+                  + sizeof(uint32_t) * MAX_PASSES == 16432,
+              "SortControl layout");
 
 // Pass plan of a plain sort, one word per digit pass, written by the histogram's last CTA.
 // A pass whose digit is the same for every key (one digit holds all n keys) is the identity
@@ -61,6 +66,15 @@ struct KernelGate
 {
   const uint32_t* gate;
   uint32_t gate_mask;
+  uint32_t pad0;
+};
+
+// Folds the bits `mask` of a sub-sort's status word into its caller's (one thread).
+struct StatusFoldParams
+{
+  uint32_t* dst;
+  const uint32_t* src;
+  uint32_t mask;
   uint32_t pad0;
 };
 
@@ -142,7 +156,8 @@ constexpr int SEG_MAX_PASSES = 12; // 8-bit digits, plus one split pass to match
 // Counter words at the start of the segmented sort's temporary storage (zeroed per call).
 enum : uint32_t
 {
-  SEG_CTR_SMALL = 0, // segments per class
+  SEG_CTR_STATUS = 0, // STATUS_* bits: word 0 of the temporary storage, as in every sort
+  SEG_CTR_SMALL,      // segments per class
   SEG_CTR_MEDIUM,
   SEG_CTR_BLOCK_S,
   SEG_CTR_BLOCK_L,
@@ -155,11 +170,10 @@ enum : uint32_t
   SEG_CTR_TICKET_HIST,
   SEG_CTR_TICKET_SCAN,
   SEG_CTR_TICKET_PASS0, // one per device pass
-  SEG_CTR_COUNT        = SEG_CTR_TICKET_PASS0 + 16,
-  SEG_CTR_DEVICE_ITEMS = SEG_CTR_COUNT, // u64 (two words): keys in device-class segments
-  SEG_CTR_STATUS       = 31,
+  SEG_CTR_DEVICE_ITEMS = 30, // u64 (two words, 8-byte aligned): keys in device-class segments
   SEG_CTR_WORDS        = 32
 };
+static_assert(SEG_CTR_TICKET_PASS0 + SEG_MAX_PASSES <= SEG_CTR_DEVICE_ITEMS, "segmented counter words overlap");
 
 struct DeviceSegment
 {

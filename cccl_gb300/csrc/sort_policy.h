@@ -56,9 +56,21 @@ GB300_HD constexpr int persistent_main(int kb, int vb)
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
 constexpr int HISTOGRAM_TPB    = 512;
-// CTAs per SM the plain histogram's registers are sized for (32 registers a thread): it is
-// bound by shared-memory atomics, and at 40 registers (three CTAs per SM) it ran 20-40 % slower
+// CTAs per SM the CTA-table histogram's registers are sized for (32 registers a thread): it
+// is bound by shared-memory atomics, and at 40 registers (three CTAs per SM) it ran 20-40 %
+// slower. The plain sort uses the lane-column histogram below; this one serves the
+// allocation-free entry point and the learned sort's bucket-id histogram.
 constexpr int HISTOGRAM_MINB   = 4;
+
+// Lane-column histogram of the plain sort (histogram_lanes_body): one CTA of 1024 threads per
+// SM; every lane owns a column of 32-bit counters per (pass, digit), so the 32 increments of
+// one warp instruction hit 32 different banks. Passes 0-3 get 32 columns (32 KB each), passes
+// 4-7 share 16 columns (16 KB each, two lanes per column: a two-way conflict).
+constexpr int HISTOGRAM_LANES_TPB = 1024;
+GB300_HD constexpr size_t histogram_table_bytes(int passes)
+{
+  return passes <= 2 ? size_t(65536) : passes <= 4 ? size_t(131072) : size_t(196608);
+}
 
 GB300_HD constexpr int onesweep_items(int kb, int vb)
 {

@@ -150,6 +150,55 @@ __device__ __forceinline__ void warp_rank_stable(
   }
 }
 
+// Stable tile positions with the peer lanes found through shared memory instead of ballots:
+// every lane ORs its lane bit into tbl_w[digit] (one word per digit for the warp), the warp
+// re-reads its word to get the lanes sharing its digit, and the highest of them advances the
+// digit's running offset and clears the word again. Three shared-memory operations per key
+// in place of eight ballots: the ballots run on the integer ALU pipe, which the ballot form
+// keeps saturated, these on the load/store pipe. tbl_w (256 words) must be zero on entry and
+// is zero again on return. ALT = true ranks every other item (odd i) this way and the rest by
+// ballots, splitting the work between the two pipes.
+template <class U, int FP, int ITEMS, bool ALT>
+__device__ __forceinline__ void warp_rank_stable_table(
+  const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, uint32_t* tbl_w, int bit, uint32_t dmask)
+{
+  const int lane    = threadIdx.x & 31;
+  const uint32_t le = lanemask_le();
+  const uint32_t me = 1u << lane;
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+  {
+    const uint32_t d = extract_digit<U, FP>(keys[i], bit, dmask);
+    uint32_t peers;
+    if (ALT && (i & 1) == 0)
+    {
+      peers = warp_match_digit(d);
+    }
+    else
+    {
+      volatile uint32_t* slot = tbl_w + d;
+      atomicOr(const_cast<uint32_t*>(slot), me);
+      __syncwarp();
+      peers = *slot;
+      __syncwarp(); // every lane has read its word before a leader clears it
+    }
+    const int leader      = 31 - __clz(peers);
+    const uint32_t cnt_le = __popc(peers & le);
+    uint32_t base         = 0;
+    if (lane == leader)
+    {
+      base = atomicAdd(&whist_w[d], cnt_le);
+      if (!(ALT && (i & 1) == 0))
+      {
+        tbl_w[d] = 0u;
+      }
+    }
+    base   = __shfl_sync(0xffffffffu, base, leader);
+    pos[i] = base + cnt_le - 1;
+  }
+  __syncwarp(); // the clears are visible before the table is reused
+}
+
 // The same two steps for digits computed by the caller (dig[i] < 256), used by passes
 // whose digit is not a bit field of the key.
 template <int ITEMS>

@@ -245,3 +245,20 @@ def radix_sort(
         end_bit=end_bit,
         stream=stream,
     )
+
+
+def sort_status(temp_storage=None, stream=None) -> tuple[int, int]:
+    """Waits for ``stream`` and returns ``(CUresult, status bits)`` of the sort that last ran
+    with ``temp_storage`` (cccl_gb300_sort_status): CUDA_SUCCESS, or CUDA_ERROR_LAUNCH_TIMEOUT
+    when a bounded wait on the GPU ran out (the result is then incomplete), or
+    CUDA_ERROR_INVALID_VALUE for segments the segmented sort could not take. The word is
+    cleared. ``temp_storage=None`` reads the allocation-free entry point's status."""
+    lib = B.load_library()
+    bits = C.c_uint32(0)
+    if temp_storage is None:
+        ptr, nbytes = None, 0
+    else:
+        ptr, nbytes = temp_storage.data_ptr(), temp_storage.numel() * temp_storage.element_size()
+    rc = lib.cccl_gb300_sort_status(ptr, nbytes, _stream_handle(stream), C.byref(bits))
+    return rc, bits.value
+

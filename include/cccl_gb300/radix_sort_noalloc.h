@@ -7,7 +7,8 @@
  * that runs inside a host framework or service with a fixed device-memory budget may not be
  * allowed to allocate outside that budget at all. This entry point needs no temporary
  * storage argument: its scratch space is a fixed array of device memory inside the library
- * (about 8.4 MB per GPU, held by every GPU that loads the library until the process exits).
+ * (CCCL_GB300_NOALLOC_SCRATCH_BYTES = 8,763,648 bytes, 8.36 MiB, held in every CUDA context
+ * that loads the library until the context is destroyed or the process exits).
  *
  * Limits and behaviour:
  *  - num_items <= CCCL_GB300_NOALLOC_MAX_ITEMS; larger inputs are rejected with
@@ -16,12 +17,16 @@
  *    (the inputs are not modified); pass NULL values for a keys-only sort;
  *  - order and [begin_bit, end_bit) follow cccl_device_radix_sort; the output is
  *    identical to cccl_device_radix_sort's for the same arguments;
- *  - the first call on a device looks up the scratch array's device address (and sets
- *    kernel attributes) for that device; make that first call before any stream capture;
- *  - every call uses the same scratch array, so calls whose work overlaps on the GPU
- *    (different streams, or different host threads on one device) race and corrupt each
- *    other's results: order them on one stream or synchronize between them;
- *  - work is enqueued on `stream` and the call returns without waiting for it.
+ *  - it runs in the CUDA context current on the calling thread (the runtime's primary
+ *    context of the current device when none is); the first call in each context looks up
+ *    that context's copy of the scratch array (and sets kernel attributes); make that first
+ *    call before any stream capture;
+ *  - every call in a context uses the same scratch array, so calls whose work overlaps on
+ *    the GPU (different streams, or different host threads on one device) race and corrupt
+ *    each other's results: order them on one stream or synchronize between them;
+ *  - work is enqueued on `stream` and the call returns without waiting for it;
+ *    cccl_gb300_sort_status(NULL, 0, stream, &bits) (sort_status.h) waits for it and
+ *    reports whether a bounded wait inside the sort ran out.
  */
 #pragma once
 
@@ -38,6 +43,7 @@
 #endif
 
 #define CCCL_GB300_NOALLOC_MAX_ITEMS (1u << 20)
+#define CCCL_GB300_NOALLOC_SCRATCH_BYTES 8763648u
 
 CCCL_C_EXTERN_C_BEGIN
 

@@ -149,3 +149,60 @@ def gpu_seg_sort(keys, values, begin, end, descending=False, overwrite=False, of
         sel = None
         kout, vout = ko, vo
     return from_dev(kout, keys.dtype), (from_dev(vout, values.dtype) if values is not None else None), sel
+
+
+def radix_order(t: torch.Tensor, kind: str, descending: bool = False) -> torch.Tensor:
+    """int64 ranks of a key tensor in CUB's radix order, computed with plain torch integer
+    operations (an independent check of the engine): unsigned / signed integer order, floats
+    by their bit order with -0.0 equal to +0.0 (cub/cub/util_type.cuh:893-963,
+    cub/cub/block/radix_rank_sort_operations.cuh:43-80), NaNs placed by their bits.
+    Descending order reverses the ranks. kind is "u", "i" or "f"."""
+    size = t.element_size()
+    raw = t.view({1: torch.int8, 2: torch.int16, 4: torch.int32, 8: torch.int64}[size])
+    min64 = torch.iinfo(torch.int64).min
+    if kind == "i":
+        o = raw.long()
+    elif size < 8:
+        bits = 8 * size
+        u = raw.long() & ((1 << bits) - 1)  # the unsigned bit pattern
+        if kind == "f":
+            sign = 1 << (bits - 1)
+            u = torch.where(u == sign, torch.zeros_like(u), u)  # -0.0 ranks with +0.0
+            u = torch.where(u >= sign, u ^ ((1 << bits) - 1), u | sign)
+        o = u
+    else:
+        o = raw.clone()
+        if kind == "f":
+            o = torch.where(o == min64, torch.zeros_like(o), o)
+            o = o ^ ((o >> 63) | min64)  # sortable unsigned bits
+        o = o ^ min64  # unsigned order as signed int64
+    return ~o if descending else o
+
+
+def check_sorted_pairs(keys_in: torch.Tensor, keys_out: torch.Tensor, values_out: torch.Tensor, kind: str,
+                       descending: bool = False) -> bool:
+    """True when keys_out/values_out are the stable radix sort of keys_in with values equal to
+    the input index: keys in order, equal keys in index order, values a permutation of the
+    indices, and every output key the input key its value names (bit for bit). Together these
+    fix the output uniquely. Runs on the GPU."""
+    n = keys_in.numel()
+    if n == 0:
+        return True
+    o = radix_order(keys_out, kind, descending)
+    if not bool((o[1:] >= o[:-1]).all()):
+        return False
+    idx = values_out.long()
+    if n > 1:
+        eq = o[1:] == o[:-1]
+        if not bool((idx[1:][eq] > idx[:-1][eq]).all()):
+            return False
+    del o
+    if bool(((idx < 0) | (idx >= n)).any()):
+        return False
+    seen = torch.zeros(n, dtype=torch.bool, device=keys_in.device)
+    seen[idx] = True
+    if not bool(seen.all()):
+        return False
+    size = keys_in.element_size()
+    w = {1: torch.int8, 2: torch.int16, 4: torch.int32, 8: torch.int64}[size]
+    return bool((keys_in.view(w)[idx] == keys_out.view(w)).all())

@@ -169,14 +169,65 @@ def test_c_abi_reference_cases(oracle):
 
 
 def test_status_word_clean_after_sort():
+    """The exported status query reads word 0 of the call's temp storage: no error after a
+    normal sort (onesweep path), and none after a single-tile sort that reuses the buffer."""
     import torch
 
+    from cccl_gb300 import _bindings as B, sort_status
     from gpu_util import gpu_sort
 
     k = I.uniform_bits(np.uint32, 3_000_000, np.random.default_rng(5))
     _, _, _, temp = gpu_sort(k, None, return_temp=True)
-    status = temp[: 16 * 1024 + 8].view(torch.int32)[4097].item()  # SortControl::status
-    assert status == 0
+    rc, bits = sort_status(temp)
+    assert (rc, bits) == (B.CUDA_SUCCESS, 0)
+    temp.view(torch.int32)[0] = B.STATUS_WAIT_TIMEOUT  # a stale word from an earlier call ...
+    from cccl_gb300 import SortOrder, make_radix_sort
+    from gpu_util import to_dev
+
+    small = to_dev(k[:1000])
+    out = torch.empty_like(small)
+    s = make_radix_sort(d_in_keys=small, d_out_keys=out, d_in_values=None, d_out_values=None,
+                        order=SortOrder.ASCENDING)
+    s(temp_storage=temp, d_in_keys=small, d_out_keys=out, d_in_values=None, d_out_values=None, num_items=1000)
+    assert sort_status(temp) == (B.CUDA_SUCCESS, 0)  # ... is cleared by the next call
+
+
+def test_wait_timeout_is_reported_and_the_gpu_stays_usable(oracle):
+    """The failure path of the bounded look-back wait, without a GPU fault: one tile of every
+    digit pass withholds its counts (a test hook of the loaded kernels), the wait limit is
+    1 ms, so its successors' waits run out. The sort returns, the status query reports
+    CUDA_ERROR_LAUNCH_TIMEOUT, and the next sort on the same GPU and build is bit-exact."""
+    import ctypes as C
+
+    import torch
+
+    from cccl_gb300 import _bindings as B, SortOrder, make_radix_sort, sort_status
+    from gpu_util import from_dev, to_dev
+
+    lib = B.load_library()
+    rng = np.random.default_rng(99)
+    n = 1 << 22
+    k = I.uniform_bits(np.uint32, n, rng)
+    v = I.index_values(n)
+    kd, vd = to_dev(k), to_dev(v)
+    ko, vo = torch.empty_like(kd), torch.empty_like(vd)
+    args = dict(d_in_keys=kd, d_out_keys=ko, d_in_values=vd, d_out_values=vo)
+    s = make_radix_sort(order=SortOrder.ASCENDING, **args)
+    temp = torch.empty(s(temp_storage=None, num_items=n, **args), dtype=torch.uint8, device="cuda")
+    library = C.c_void_p(s.build_result.library)
+    assert lib.cccl_gb300_testing_set_wait_fault(library, 5, 1_000_000) == B.CUDA_SUCCESS
+    try:
+        s(temp_storage=temp, num_items=n, **args)
+        rc, bits = sort_status(temp)
+        assert rc == B.CUDA_ERROR_LAUNCH_TIMEOUT and bits & B.STATUS_WAIT_TIMEOUT
+        assert sort_status(temp) == (B.CUDA_SUCCESS, 0)  # read and cleared
+    finally:
+        assert lib.cccl_gb300_testing_set_wait_fault(library, 0xFFFFFFFF, 1_000_000_000) == B.CUDA_SUCCESS
+    s(temp_storage=temp, num_items=n, **args)
+    assert sort_status(temp) == (B.CUDA_SUCCESS, 0)
+    rk, rv = oracle.radix_sort(k, v, threads=4)
+    assert from_dev(ko, np.uint32).tobytes() == rk.tobytes()
+    assert from_dev(vo, np.uint32).tobytes() == rv.tobytes()
 
 
 def test_large_full_size_properties():

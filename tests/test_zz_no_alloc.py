@@ -52,10 +52,19 @@ def _noalloc(lib, keys, values=None, b=0, e=32, desc=False):
 
 CASES = [
     (1000, True, 0, 32, False),      # single-tile path
+    (4865, False, 0, 32, False),     # one past the single-tile cut: the smallest multi-pass sort
+    (4865, True, 0, 32, True),
     (300_001, False, 0, 32, False),  # 4 passes, keys only
     (300_001, True, 0, 32, True),    # pairs, descending
+    (300_001, True, 7, 7, False),    # begin_bit == end_bit: a copy
     (1 << 20, True, 4, 27, False),   # the maximum size, a bit window (3 passes)
 ]
+
+
+def _status_clean():
+    from cccl_gb300 import _bindings as B, sort_status
+
+    assert sort_status(None) == (B.CUDA_SUCCESS, 0)  # the built-in array's status word
 
 
 @pytest.mark.parametrize("n,with_values,b,e,desc", CASES)
@@ -67,10 +76,38 @@ def test_noalloc_matches_regular_entry_point(lib, n, with_values, b, e, desc):
         keys = I.entropy_reduced(np.uint32, n, rng, 1 + call)
         values = rng.integers(0, 2**32, size=n, dtype=np.uint32) if with_values else None
         ko, vo = _noalloc(lib, keys, values, b, e, desc)
+        _status_clean()
         rk, rv, _ = gpu_sort(keys, values, b, e, desc)
         assert ko.tobytes() == rk.tobytes()
         if with_values:
             assert vo.tobytes() == rv.tobytes()
+
+
+def test_noalloc_keys_then_pairs(lib):
+    """A keys-only call and then a pairs call of another size: the two use different tile
+    sizes (so different numbers of look-back rows in the shared array) and must not see
+    each other's leftovers."""
+    from gpu_util import gpu_sort
+
+    rng = np.random.default_rng(4242)
+    for n, with_values in ((700_001, False), (250_003, True), (900_000, False)):
+        keys = I.uniform_bits(np.uint32, n, rng)
+        values = I.index_values(n) if with_values else None
+        ko, vo = _noalloc(lib, keys, values)
+        _status_clean()
+        rk, rv, _ = gpu_sort(keys, values)
+        assert ko.tobytes() == rk.tobytes()
+        if with_values:
+            assert vo.tobytes() == rv.tobytes()
+
+
+def test_noalloc_empty_input(lib):
+    import torch
+
+    rc = lib.cccl_gb300_radix_sort_u32_noalloc(None, None, None, None, 0, 0, 32, False,
+                                               torch.cuda.current_stream().cuda_stream)
+    assert rc == 0
+    _status_clean()
 
 
 def test_noalloc_rejects_too_many_items(lib):
