@@ -269,8 +269,10 @@ def segmented_workload(seed=77, total=1 << 27):
     return k, v, b.astype(np.int32), e.astype(np.int32)
 
 
-def run_segmented(torch, steps, per_segment_sample=4000):
-    """Batched segmented sort vs one plain radix-sort launch per segment (same GPU)."""
+def run_segmented(torch, steps, per_segment_sample=None):
+    """Batched segmented sort vs one plain radix-sort launch per segment (same GPU). The
+    per-segment bar sorts every non-empty segment of the batch with its own plain sort call
+    (per_segment_sample limits it to a sample, for profiling runs only)."""
     import numpy as np
 
     from cccl_gb300 import SortOrder, make_radix_sort, make_segmented_sort
@@ -310,7 +312,7 @@ def run_segmented(torch, steps, per_segment_sample=4000):
     # one plain radix SortPairs launch per segment, on a sample of the segments
     sizes = e - b
     idx = np.nonzero(sizes > 0)[0]
-    sample = idx[:: max(1, idx.size // per_segment_sample)]
+    sample = idx if per_segment_sample is None else idx[:: max(1, idx.size // per_segment_sample)]
     rs = make_radix_sort(d_in_keys=kd, d_out_keys=ko, d_in_values=vd, d_out_values=vo, order=SortOrder.ASCENDING)
     max_seg = int(sizes.max())
     tb = max(rs(temp_storage=None, d_in_keys=kd[:max_seg], d_out_keys=ko[:max_seg], d_in_values=vd[:max_seg],
@@ -324,7 +326,7 @@ def run_segmented(torch, steps, per_segment_sample=4000):
 
     ps_ms = time_steps(torch, per_segment, 1, 1, lambda: None)
     sample_items = int(sizes[sample].sum())
-    # scale the sample to the whole batch by its share of segments (launch-bound) and keys
+    # measured over every segment; a profiling sample is scaled by its share of segments
     ps_full_ms = ps_ms * max(idx.size / sample.size, 1.0)
     peak, _ = _peaks()
     alg_bytes = 4 * n * 2 * 8
@@ -340,9 +342,9 @@ def run_segmented(torch, steps, per_segment_sample=4000):
         "roofline_frac_one_pass_floor": (n * 16) / (ms / 1e3) / 1e9 / peak,
         "kernel_ms": kt,
         "launches_per_call": launches,
-        "per_segment_launch_ms_sample": ps_ms,
-        "per_segment_sample": {"segments": int(sample.size), "keys": sample_items},
-        "per_segment_launch_ms_estimated_full": ps_full_ms,
+        "per_segment_launch_ms": ps_full_ms,
+        "per_segment_launch_measured": {"segments": int(sample.size), "keys": sample_items,
+                                        "all_segments": bool(sample.size == idx.size)},
         "speedup_vs_per_segment_launches": ps_full_ms / ms,
     }
 
@@ -421,7 +423,10 @@ def run_learned(torch, reps):
         kb, vb = k0.element_size(), v0.element_size()
         res = {"workload": f"{label}, {dist}", "num_items": n}
         results = {}
-        for method, maker in (("plain", make_radix_sort), ("learned", make_learned_sort)):
+        methods = [("plain", make_radix_sort), ("learned", make_learned_sort)]
+        if kb == 4:  # the cost model sends 4-byte keys to the plain sort: time the learned kernels too
+            methods.append(("learned_forced", lambda **a: make_learned_sort(route="always", **a)))
+        for method, maker in methods:
             k, v = (k0.clone(), v0.clone()) if overwrite else (k0, v0)
             ko, vo = torch.empty_like(k0), torch.empty_like(v0)
             if overwrite:
@@ -443,8 +448,8 @@ def run_learned(torch, reps):
             res[method + "_ms"] = ms
             res[method + "_keys_per_s"] = n / (ms / 1e3)
             res[method + "_kernel_ms"] = {r: round(t, 4) for r, t in kt.items()}
-            if method == "learned":
-                res["learned_stats"] = s.stats(temp_storage=tmp, num_items=n, **args)
+            if method.startswith("learned"):
+                res[method + "_stats"] = s.stats(temp_storage=tmp, num_items=n, **args)
             if overwrite:
                 results[method] = (dk.current().clone(), dv.current().clone(), dk.selector)
             else:
@@ -455,6 +460,11 @@ def run_learned(torch, reps):
         lk, lv, lsel = results["learned"]
         res["bitexact_vs_plain"] = bool(torch.equal(pk.view(torch.uint8), lk.view(torch.uint8))
                                         and torch.equal(pv, lv) and psel == lsel)
+        if "learned_forced" in results:
+            fk, fv, fsel = results["learned_forced"]
+            res["learned_forced_bitexact_vs_plain"] = bool(torch.equal(pk.view(torch.uint8), fk.view(torch.uint8))
+                                                           and torch.equal(pv, fv) and psel == fsel)
+            res["learned_forced_speedup_vs_plain"] = res["plain_ms"] / res["learned_forced_ms"]
         # the plain result itself against an independent check (order, stability, permutation)
         res["plain_verified"] = check_sorted_pairs(k0, pk, pv, "f")
         full_passes = 8 * kb // 8
@@ -465,9 +475,12 @@ def run_learned(torch, reps):
         res["roofline_frac_plain_bytes"] = {
             m: (plain_bytes / (res[m + "_ms"] / 1e3) / 1e9 / peak if res["plain_passes_run"] == full_passes else None)
             for m in ("plain", "learned")}
-        st = res["learned_stats"]
-        learned_bytes = (st["partition_passes"] + 1) * n * 2 * (kb + vb)
-        res["roofline_frac_learned_bytes"] = learned_bytes / (res["learned_ms"] / 1e3) / 1e9 / peak
+        # the learned route's own bytes (partition passes + the bucket sort), where it ran
+        for m in [m for m, _ in methods if m.startswith("learned")]:
+            st = res[m + "_stats"]
+            learned_bytes = (st["partition_passes"] + 1) * n * 2 * (kb + vb)
+            res["roofline_frac_learned_bytes" + m[len("learned"):]] = (
+                learned_bytes / (res[m + "_ms"] / 1e3) / 1e9 / peak if st["learned"] else None)
         out.append(res)
         del k0, v0, results, pk, pv, lk, lv
         torch.cuda.empty_cache()

@@ -194,6 +194,7 @@ EXPORTED_SYMBOLS = [
     "cccl_gb300_learned_sort",
     "cccl_gb300_learned_sort_stats",
     "cccl_gb300_learned_sort_cleanup",
+    "cccl_gb300_learned_sort_set_route",
     "cccl_gb300_segmented_radix_sort",
     "cccl_gb300_sort_status",
     "cccl_gb300_testing_set_wait_fault",
@@ -289,6 +290,7 @@ def _declare(lib):
         P(LearnedSortStats),
     ]
     lib.cccl_gb300_learned_sort_cleanup.argtypes = [L]
+    lib.cccl_gb300_learned_sort_set_route.argtypes = [L, C.c_int]
     lib.cccl_gb300_sort_status.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, P(C.c_uint32)]
     lib.cccl_gb300_testing_set_wait_fault.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64]
     for name in EXPORTED_SYMBOLS:

@@ -145,6 +145,8 @@ inline bool supported_value_bytes(size_t vb)
 // Encoding of raw key bits to the sortable unsigned order, with descending order folded
 // in as a bit inversion (cub/cub/util_type.cuh:893-963 and
 // cub/cub/block/radix_rank_sort_operations.cuh:536-575 define the mapping).
+// Integer kinds get fwd_pos == fwd_neg (one mask for both signs): the integer kernels'
+// counting loops encode with fwd_pos alone (encode_key_for_count).
 inline KeyCodec make_codec(int kind, int bytes, bool descending)
 {
   const unsigned long long all  = bytes == 8 ? ~0ull : ((1ull << (8 * bytes)) - 1ull);

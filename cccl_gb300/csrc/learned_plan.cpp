@@ -90,6 +90,18 @@ LearnedTempPlan plan_learned_temp(const LearnedSetup& s, const RadixCall& c)
   t.bucket_log2        = std::clamp(ceil_log2(n) - items_log2, 8, LEARNED_MAX_BUCKET_LOG2);
   t.bucket_cap         = 2 << items_log2;
   t.passes         = (t.bucket_log2 + RADIX_BITS - 1) / RADIX_BITS;
+  // Cost model. The learned route moves about (partition passes + 1 bucket-sort pass) times
+  // 2 (K + V) bytes per key, the plain sort K passes of the same (8-bit digits of a K-byte
+  // key), and the learned kernels ran at about 0.7 of the plain passes' bandwidth on GB300
+  // (model evaluation per key, in-shared-memory bucket sort). So it takes the learned route
+  // only when (passes + 1) / 0.7 < K: 8-byte keys (3 + 1 against 8 passes), never 4-byte keys
+  // (2 + 1 against 4). Inputs it sends to the plain sort cost nothing extra.
+  if (s.route_policy == LEARNED_POLICY_COST_MODEL && (t.passes + 1) * 10 >= kb * 7)
+  {
+    t         = LearnedTempPlan{};
+    t.learned = false;
+    return t;
+  }
   t.tile_items     = persistent_tile_items(s.pass_tpb, s.pass_items);
   t.portion_items  = ((1ull << 30) - 1) / t.tile_items * t.tile_items; // 30-bit look-back counts
   t.num_portions   = ceil_div(n, t.portion_items);

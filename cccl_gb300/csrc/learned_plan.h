@@ -49,7 +49,13 @@ struct LearnedSetup
   SegmentedPolicy seg_pol; // bucket sort
   SegmentedKernels seg_ks;
   LearnedKernels lk;
+  int32_t route_policy; // LEARNED_POLICY_*
+  int32_t reserved0;
 };
+
+// Host-side route policy of a build (cccl_gb300_learned_sort_set_route).
+constexpr int LEARNED_POLICY_COST_MODEL = 0; // learned only where its byte count predicts a win
+constexpr int LEARNED_POLICY_ALWAYS     = 1; // learned wherever the input qualifies
 
 // Where the pieces of one call live in its temporary storage.
 struct LearnedTempPlan

@@ -152,6 +152,7 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_build(
     s->pass_tpb    = persistent_tpb(kb, int(vb));
     s->pass_items  = learned_items(kb, int(vb));
     s->pass_smem   = learned_pass_smem(kb, int(vb));
+    s->route_policy = LEARNED_POLICY_COST_MODEL;
 
     auto load = [](CUlibrary* lib, const image_ref& img) {
       check(cuLibraryLoadData(lib, img.data, nullptr, nullptr, 0, nullptr, nullptr, 0), "cuLibraryLoadData");
@@ -289,6 +290,22 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_stats(
   {
     return report("cccl_gb300_learned_sort_stats", e);
   }
+}
+
+CCCL_GB300_API CUresult cccl_gb300_learned_sort_set_route(cccl_gb300_learned_sort_build_result_t* build, int route)
+{
+  if (build == nullptr || build->setup == nullptr || build->setup_size != sizeof(LearnedSetup)
+      || (route != CCCL_GB300_LEARNED_ROUTE_COST_MODEL && route != CCCL_GB300_LEARNED_ROUTE_ALWAYS))
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  auto* s = static_cast<LearnedSetup*>(build->setup);
+  if (s->magic != SETUP_MAGIC)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  s->route_policy = route == CCCL_GB300_LEARNED_ROUTE_ALWAYS ? LEARNED_POLICY_ALWAYS : LEARNED_POLICY_COST_MODEL;
+  return CUDA_SUCCESS;
 }
 
 CCCL_GB300_API CUresult cccl_gb300_learned_sort_cleanup(cccl_gb300_learned_sort_build_result_t* build)

@@ -997,7 +997,14 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
             tbl[k] = 0u;
           }
           __syncwarp();
-          warp_rank_stable_table<U, FP, ITEMS, GB300_RANK_MODE == 2>(keys, pos, whist + warp * R, tbl, bit, dmask);
+          if constexpr (GB300_RANK_MODE == 3)
+          {
+            warp_rank_stable_adaptive<U, FP, ITEMS>(keys, pos, whist + warp * R, tbl, bit, dmask);
+          }
+          else
+          {
+            warp_rank_stable_table<U, FP, ITEMS, GB300_RANK_MODE == 2>(keys, pos, whist + warp * R, tbl, bit, dmask);
+          }
         }
         else if constexpr (STABLE)
         {

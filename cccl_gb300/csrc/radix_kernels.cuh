@@ -257,13 +257,114 @@ __device__ __forceinline__ void histogram_body(const HistogramParams& p)
 // (the adds are atomic). At the end each row of columns is summed by a warp and the totals go
 // to histogram_finish. Keys are streamed with four 16-byte loads in flight per thread.
 // ---------------------------------------------------------------------------------------
+// Encoded key for the counting loops: integer kinds have one mask for both signs (make_codec),
+// so their encoding is a single XOR; floating-point kinds pick the mask by the sign bit.
+template <class U, int FP>
+__device__ __forceinline__ U encode_key_for_count(U x, const KeyCodec& c)
+{
+  if constexpr (FP == FP_NONE)
+  {
+    return U(x ^ U(c.fwd_pos));
+  }
+  else
+  {
+    return encode_key<U>(x, c);
+  }
+}
+
+// Counts one key's digits in passes [0, NP): digit q is byte q of t (the key's window,
+// shifted down to bit 0), its counter address one byte permute away (see the layout above).
+template <class U, int NP>
+__device__ __forceinline__ void count_digits_lanes(U t, uint32_t table_base, const uint32_t (&col)[8])
+{
+  const uint32_t lo = uint32_t(t);
+  uint32_t hi       = 0;
+  if constexpr (sizeof(U) == 8)
+  {
+    hi = uint32_t((unsigned long long) t >> 32);
+  }
+#pragma unroll
+  for (int q = 0; q < NP; ++q)
+  {
+    const uint32_t off = __byte_perm(q < 4 ? lo : hi, col[q], 0x7604u | (uint32_t(q & 3) << 4));
+    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(table_base + off));
+  }
+}
+
+template <int KB, int FP, int TPB, int NP, bool WINDOW>
+__device__ __forceinline__ void histogram_lanes_count(const HistogramParams& p, uint32_t table_base, const uint32_t (&col)[8])
+{
+  using U           = typename uint_of<KB>::type;
+  constexpr int VEC = 16 / KB; // keys per 16-byte load
+  const int tid     = threadIdx.x;
+  const int bb      = p.begin_bit;
+  const int wbits   = p.end_bit - p.begin_bit;
+  const U wmask     = wbits >= 8 * KB ? U(~U(0)) : U((U(1) << wbits) - U(1));
+  auto count_key    = [&](U raw) {
+    U t = digit_source<U, FP>(encode_key_for_count<U, FP>(raw, p.codec));
+    if constexpr (WINDOW)
+    {
+      t = U(U(t >> bb) & wmask);
+    }
+    count_digits_lanes<U, NP>(t, table_base, col);
+  };
+  const U* keys                 = static_cast<const U*>(p.keys);
+  const unsigned long long n    = p.num_items;
+  const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
+  unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
+  if (head > n)
+  {
+    head = n;
+  }
+  const unsigned long long nvec     = (n - head) / VEC;
+  const unsigned long long body_end = head + nvec * VEC;
+  if (blockIdx.x == 0)
+  {
+    for (unsigned long long i = tid; i < head; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+    for (unsigned long long i = body_end + tid; i < n; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+  }
+  const uint4* vkeys              = reinterpret_cast<const uint4*>(keys + head);
+  const unsigned long long stride = (unsigned long long) gridDim.x * TPB;
+  unsigned long long v            = blockIdx.x * (unsigned long long) TPB + tid;
+  auto count_vec                  = [&](const uint4& w) {
+    U k[VEC];
+    memcpy(k, &w, 16);
+#pragma unroll
+    for (int j = 0; j < VEC; ++j)
+    {
+      count_key(k[j]);
+    }
+  };
+  for (; v + 3 * stride < nvec; v += 4 * stride)
+  {
+    uint4 w[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+      w[j] = __ldcs(vkeys + v + j * stride);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+    {
+      count_vec(w[j]);
+    }
+  }
+  for (; v < nvec; v += stride)
+  {
+    count_vec(__ldcs(vkeys + v));
+  }
+}
+
 template <int KB, int FP, int TPB>
 __device__ __forceinline__ void histogram_lanes_body(const HistogramParams& p)
 {
-  using U           = typename uint_of<KB>::type;
-  constexpr int R   = RADIX_DIGITS;
-  constexpr int QN  = KB;          // passes of a whole key
-  constexpr int VEC = 16 / KB;     // keys per 16-byte load
+  constexpr int R = RADIX_DIGITS;
   extern __shared__ __align__(16) unsigned char table[];
   __shared__ uint32_t sh[MAX_PASSES * R];
   if (!gate_open(p.gate))
@@ -278,102 +379,34 @@ __device__ __forceinline__ void histogram_lanes_body(const HistogramParams& p)
   {
     *reinterpret_cast<uint4*>(table + i) = make_uint4(0u, 0u, 0u, 0u);
   }
-  uint32_t col[QN]; // byte 0 and byte 2 of every pass's counter offsets for this lane
+  uint32_t col[8]; // byte 0 and byte 2 of every pass's counter offsets for this lane
 #pragma unroll
-  for (int q = 0; q < QN; ++q)
+  for (int q = 0; q < 8; ++q)
   {
     col[q] = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(q & 1) * 128u + uint32_t(lane) * 4u))
                    : ((2u << 16) | (uint32_t(q & 3) * 64u + uint32_t(lane & 15) * 4u));
   }
+  const uint32_t table_base = smem_addr(table);
   __syncthreads();
 
-  const int bb        = p.begin_bit;
-  const int wbits     = p.end_bit - p.begin_bit;
-  const U wmask       = wbits >= 8 * KB ? U(~U(0)) : U((U(1) << wbits) - U(1));
-  const bool windowed = bb != 0 || wbits != 8 * KB;
-  auto count_key = [&](U raw, auto window_tag) {
-    U t = digit_source<U, FP>(encode_key<U>(raw, p.codec));
-    if constexpr (decltype(window_tag)::value)
-    {
-      t = U(U(t >> bb) & wmask);
-    }
-    const uint32_t lo = uint32_t(t);
-    uint32_t hi       = 0;
-    if constexpr (KB == 8)
-    {
-      hi = uint32_t((unsigned long long) t >> 32);
-    }
-#pragma unroll
-    for (int q = 0; q < QN; ++q)
-    {
-      if (q < P)
-      {
-        // byte 0 and byte 2 from the lane's column word, byte 1 = digit q, byte 3 = 0
-        const uint32_t off = __byte_perm(q < 4 ? lo : hi, col[q], 0x7604u | (uint32_t(q & 3) << 4));
-        atomicAdd(reinterpret_cast<uint32_t*>(table + off), 1u);
-      }
-    }
-  };
-  auto count_all = [&](auto window_tag) {
-    const U* keys                 = static_cast<const U*>(p.keys);
-    const unsigned long long n    = p.num_items;
-    const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
-    unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
-    if (head > n)
-    {
-      head = n;
-    }
-    const unsigned long long nvec     = (n - head) / VEC;
-    const unsigned long long body_end = head + nvec * VEC;
-    if (blockIdx.x == 0)
-    {
-      for (unsigned long long i = tid; i < head; i += TPB)
-      {
-        count_key(keys[i], window_tag);
-      }
-      for (unsigned long long i = body_end + tid; i < n; i += TPB)
-      {
-        count_key(keys[i], window_tag);
-      }
-    }
-    const uint4* vkeys                = reinterpret_cast<const uint4*>(keys + head);
-    const unsigned long long stride   = (unsigned long long) gridDim.x * TPB;
-    unsigned long long v              = blockIdx.x * (unsigned long long) TPB + tid;
-    auto count_vec = [&](const uint4& w) {
-      U k[VEC];
-      memcpy(k, &w, 16);
-#pragma unroll
-      for (int j = 0; j < VEC; ++j)
-      {
-        count_key(k[j], window_tag);
-      }
-    };
-    for (; v + 3 * stride < nvec; v += 4 * stride)
-    {
-      uint4 w[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-      {
-        w[j] = __ldcs(vkeys + v + j * stride);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-      {
-        count_vec(w[j]);
-      }
-    }
-    for (; v < nvec; v += stride)
-    {
-      count_vec(__ldcs(vkeys + v));
-    }
-  };
-  if (windowed)
+  // the pass count is a compile-time constant of the counting loop: a whole key, or a window
+  if (p.begin_bit == 0 && p.end_bit == 8 * KB)
   {
-    count_all(BoolTag<true>{});
+    histogram_lanes_count<KB, FP, TPB, KB, false>(p, table_base, col);
   }
   else
   {
-    count_all(BoolTag<false>{});
+    switch (P)
+    {
+      case 1: histogram_lanes_count<KB, FP, TPB, 1, true>(p, table_base, col); break;
+      case 2: if constexpr (KB >= 2) { histogram_lanes_count<KB, FP, TPB, 2, true>(p, table_base, col); } break;
+      case 3: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 3, true>(p, table_base, col); } break;
+      case 4: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 4, true>(p, table_base, col); } break;
+      case 5: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 5, true>(p, table_base, col); } break;
+      case 6: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 6, true>(p, table_base, col); } break;
+      case 7: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 7, true>(p, table_base, col); } break;
+      default: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 8, true>(p, table_base, col); } break;
+    }
   }
   __syncthreads();
 

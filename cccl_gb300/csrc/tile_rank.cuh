@@ -158,7 +158,7 @@ __device__ __forceinline__ void warp_rank_stable(
 // keeps saturated, these on the load/store pipe. tbl_w (256 words) must be zero on entry and
 // is zero again on return. ALT = true ranks every other item (odd i) this way and the rest by
 // ballots, splitting the work between the two pipes.
-template <class U, int FP, int ITEMS, bool ALT>
+template <class U, int FP, int ITEMS, bool ALT, int FIRST = 0>
 __device__ __forceinline__ void warp_rank_stable_table(
   const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, uint32_t* tbl_w, int bit, uint32_t dmask)
 {
@@ -166,7 +166,7 @@ __device__ __forceinline__ void warp_rank_stable_table(
   const uint32_t le = lanemask_le();
   const uint32_t me = 1u << lane;
 #pragma unroll
-  for (int i = 0; i < ITEMS; ++i)
+  for (int i = FIRST; i < ITEMS; ++i)
   {
     const uint32_t d = extract_digit<U, FP>(keys[i], bit, dmask);
     uint32_t peers;
@@ -197,6 +197,56 @@ __device__ __forceinline__ void warp_rank_stable_table(
     pos[i] = base + cnt_le - 1;
   }
   __syncwarp(); // the clears are visible before the table is reused
+}
+
+// Ranking that picks its form per warp: item 0 is ranked by ballots, and when no lane of it
+// has four or more peers (digits spread out, the common case of high-entropy keys) the
+// remaining items alternate between ballots and the lane-mask table; otherwise (many equal
+// digits, where the table's same-address ORs serialise) they all use ballots.
+template <class U, int FP, int ITEMS>
+__device__ __forceinline__ void warp_rank_stable_adaptive(
+  const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, uint32_t* tbl_w, int bit, uint32_t dmask)
+{
+  const int lane    = threadIdx.x & 31;
+  const uint32_t le = lanemask_le();
+  bool spread;
+  {
+    const uint32_t d      = extract_digit<U, FP>(keys[0], bit, dmask);
+    const uint32_t peers  = warp_match_digit(d);
+    const int leader      = 31 - __clz(peers);
+    const uint32_t cnt_le = __popc(peers & le);
+    uint32_t base         = 0;
+    if (lane == leader)
+    {
+      base = atomicAdd(&whist_w[d], cnt_le);
+    }
+    base   = __shfl_sync(0xffffffffu, base, leader);
+    pos[0] = base + cnt_le - 1;
+    spread = !__any_sync(0xffffffffu, __popc(peers) >= 4);
+  }
+  if (spread)
+  {
+    // item 1 onward: odd items by the table, even ones by ballots
+    warp_rank_stable_table<U, FP, ITEMS, true, 1>(keys, pos, whist_w, tbl_w, bit, dmask);
+  }
+  else
+  {
+#pragma unroll
+    for (int i = 1; i < ITEMS; ++i)
+    {
+      const uint32_t d      = extract_digit<U, FP>(keys[i], bit, dmask);
+      const uint32_t peers  = warp_match_digit(d);
+      const int leader      = 31 - __clz(peers);
+      const uint32_t cnt_le = __popc(peers & le);
+      uint32_t base         = 0;
+      if (lane == leader)
+      {
+        base = atomicAdd(&whist_w[d], cnt_le);
+      }
+      base   = __shfl_sync(0xffffffffu, base, leader);
+      pos[i] = base + cnt_le - 1;
+    }
+  }
 }
 
 // The same two steps for digits computed by the caller (dig[i] < 256), used by passes

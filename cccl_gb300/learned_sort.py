@@ -25,8 +25,11 @@ from .radix_sort import (
 )
 
 
+ROUTES = {"cost_model": 0, "always": 1}  # CCCL_GB300_LEARNED_ROUTE_*
+
+
 class _LearnedSort:
-    def __init__(self, d_in_keys, d_out_keys, d_in_values, d_out_values, order: SortOrder):
+    def __init__(self, d_in_keys, d_out_keys, d_in_values, d_out_values, order: SortOrder, route="cost_model"):
         ki, ko, vi, vo = _arrays(d_in_keys, d_out_keys, d_in_values, d_out_values)
         _check_device_array(ki, "d_in_keys")
         self.lib = B.load_library()
@@ -42,6 +45,8 @@ class _LearnedSort:
             minor,
         )
         check(rc, "cccl_gb300_learned_sort_build")
+        check(self.lib.cccl_gb300_learned_sort_set_route(C.byref(self.build_result), ROUTES[route]),
+              "cccl_gb300_learned_sort_set_route")
 
     def __del__(self):
         try:
@@ -136,9 +141,12 @@ class _LearnedSort:
         return {name: getattr(st, name) for name, _ in B.LearnedSortStats._fields_}
 
 
-def make_learned_sort(*, d_in_keys, d_out_keys, d_in_values, d_out_values, order: SortOrder) -> _LearnedSort:
-    """Builds a reusable learned-partition sort for the given arrays' dtypes and ``order``."""
-    return _LearnedSort(d_in_keys, d_out_keys, d_in_values, d_out_values, order)
+def make_learned_sort(*, d_in_keys, d_out_keys, d_in_values, d_out_values, order: SortOrder,
+                      route: str = "cost_model") -> _LearnedSort:
+    """Builds a reusable learned-partition sort for the given arrays' dtypes and ``order``.
+    ``route="always"`` switches the host cost model off (every qualifying input takes the
+    learned kernels); by default 4-byte keys take the plain sort."""
+    return _LearnedSort(d_in_keys, d_out_keys, d_in_values, d_out_values, order, route)
 
 
 def learned_sort(

@@ -21,6 +21,13 @@
  * sorted sample lies in buckets predicted to overflow the bucket sort, and above half
  * (near-constant keys, heavy duplicates) the plain sort runs instead. The choice is made on
  * the device, without a host synchronisation, and the result and selector are the same.
+ *
+ * Before that, a cost model on the host compares bytes moved: the partition passes plus the
+ * bucket sort against the plain sort's one pass per key byte, with the learned kernels
+ * counted at 0.7 of the plain passes' bandwidth (measured on GB300). It sends 4-byte keys to
+ * the plain sort (3 learned passes cannot beat 4 plain ones there) and takes 8-byte keys.
+ * cccl_gb300_learned_sort_set_route(build, CCCL_GB300_LEARNED_ROUTE_ALWAYS) switches the
+ * cost model off for a build (every qualifying input takes the learned kernels).
  */
 #pragma once
 
@@ -105,6 +112,12 @@ CCCL_GB300_API CUresult cccl_gb300_learned_sort_stats(
   int end_bit,
   bool is_overwrite_okay,
   cccl_gb300_learned_sort_stats_t* stats);
+
+/* Route policy of a build: CCCL_GB300_LEARNED_ROUTE_COST_MODEL (the default after
+ * cccl_gb300_learned_sort_build) or CCCL_GB300_LEARNED_ROUTE_ALWAYS. */
+#define CCCL_GB300_LEARNED_ROUTE_COST_MODEL 0
+#define CCCL_GB300_LEARNED_ROUTE_ALWAYS 1
+CCCL_GB300_API CUresult cccl_gb300_learned_sort_set_route(cccl_gb300_learned_sort_build_result_t* build, int route);
 
 CCCL_GB300_API CUresult cccl_gb300_learned_sort_cleanup(cccl_gb300_learned_sort_build_result_t* build);
 

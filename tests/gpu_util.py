@@ -58,10 +58,10 @@ def value_tensor(v: np.ndarray) -> torch.Tensor:
 
 
 def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, overwrite=False, return_temp=False,
-             method="plain", stats=None):
+             method="plain", stats=None, route="always"):
     """Sorts through cccl_device_radix_sort (method "plain") or cccl_gb300_learned_sort
-    (method "learned"; `stats`, a dict, receives the run's counters). Returns
-    (keys, values, selector[, temp])."""
+    (method "learned"; `stats`, a dict, receives the run's counters; `route` its host
+    policy, "always" or "cost_model"). Returns (keys, values, selector[, temp])."""
     from cccl_gb300 import make_learned_sort
 
     order = SortOrder.DESCENDING if descending else SortOrder.ASCENDING
@@ -77,7 +77,10 @@ def gpu_sort(keys, values=None, begin_bit=0, end_bit=None, descending=False, ove
         args = dict(d_in_keys=dk, d_out_keys=None, d_in_values=dv, d_out_values=None)
     else:
         args = dict(d_in_keys=ki, d_out_keys=ko, d_in_values=vi, d_out_values=vo)
-    sorter = (make_learned_sort if method == "learned" else make_radix_sort)(order=order, **args)
+    if method == "learned":  # route: the learned build's host policy ("always": the learned kernels)
+        sorter = make_learned_sort(order=order, route=route, **args)
+    else:
+        sorter = make_radix_sort(order=order, **args)
     nbytes = sorter(temp_storage=None, num_items=keys.size, begin_bit=begin_bit, end_bit=end_bit, **args)
     temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
     sel0 = dk.selector if overwrite else None

@@ -172,3 +172,22 @@ def test_sparse_buckets_with_specials(oracle, dtype):
     k = I.with_specials(k, rng, 1e-4)
     for desc in (False, True):
         _check(oracle, k, I.index_values(n), desc=desc)
+
+
+@pytest.mark.parametrize("dtype,expect", [(np.float32, False), (np.uint32, False), (np.float64, True),
+                                          (np.int64, True)], ids=lambda x: str(x))
+def test_cost_model_route(oracle, dtype, expect):
+    """The host cost model: 4-byte keys go to the plain sort (two partition passes and the
+    bucket sort cannot beat four plain passes), 8-byte keys take the learned kernels. The
+    result is the plain sort's either way."""
+    from gpu_util import gpu_sort
+
+    rng = np.random.default_rng(77)
+    k = (I.lognormal(dtype, N, rng) if np.dtype(dtype).kind == "f" else I.uniform_bits(dtype, N, rng))
+    v = I.index_values(N)
+    st = {}
+    ko, vo, _ = gpu_sort(k, v, method="learned", stats=st, route="cost_model")
+    rk, rv = oracle.radix_sort(k, v, threads=8)
+    assert ko.tobytes() == rk.tobytes() and vo.tobytes() == rv.tobytes()
+    assert st["learned"] == int(expect), st
+
