@@ -651,12 +651,22 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
   constexpr int TILE = L::TILE;
   static_assert(STABLE || VB == 0, "pairs need a stable pass");
   static_assert(STABLE || !Digits::computed, "computed digits are ranked stably");
-  // peers by lane-mask tables (GB300_RANK_MODE 1, or 2 for every other item) where the tables
-  // of all main warps fit in one tile buffer
-#ifndef GB300_RANK_MODE
-#  define GB300_RANK_MODE 0
+  // How the stable passes find a key's peer lanes: 0 ballots only; 1 lane-mask tables in
+  // shared memory; 2 the two alternating by item; 3 per warp, alternating where the digits
+  // are spread out and ballots where many are equal (warp_rank_stable_adaptive). The tables
+  // live in the tile's own buffer, so the mode needs all main warps' tables to fit in it.
+  // Measured on GB300 (2^28 keys, pass time): u32 keys-only 0.967 ms ballots, 0.944 / 0.905
+  // / 0.906 ms modes 1-3; u64+u32 pairs 1.693 / 1.675 / 1.674 / 1.699 ms; u64+u32 pairs of
+  // low entropy (AND of 5 words) 1.540 / 2.048 / 1.668 / 1.623 ms. Keys-only passes take
+  // mode 3, pairs keep ballots.
+#ifndef GB300_RANK_MODE_KEYS
+#  define GB300_RANK_MODE_KEYS 3
 #endif
-  constexpr bool RANK_TABLE = GB300_RANK_MODE != 0 && size_t(NW) * R * 4 <= L::buf_bytes;
+#ifndef GB300_RANK_MODE_PAIRS
+#  define GB300_RANK_MODE_PAIRS 0
+#endif
+  constexpr int RANK_MODE   = VB == 0 ? GB300_RANK_MODE_KEYS : GB300_RANK_MODE_PAIRS;
+  constexpr bool RANK_TABLE = RANK_MODE != 0 && size_t(NW) * R * 4 <= L::buf_bytes;
 
   extern __shared__ __align__(128) unsigned char smem[];
   uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
@@ -997,13 +1007,13 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
             tbl[k] = 0u;
           }
           __syncwarp();
-          if constexpr (GB300_RANK_MODE == 3)
+          if constexpr (RANK_MODE == 3)
           {
             warp_rank_stable_adaptive<U, FP, ITEMS>(keys, pos, whist + warp * R, tbl, bit, dmask);
           }
           else
           {
-            warp_rank_stable_table<U, FP, ITEMS, GB300_RANK_MODE == 2>(keys, pos, whist + warp * R, tbl, bit, dmask);
+            warp_rank_stable_table<U, FP, ITEMS, RANK_MODE == 2>(keys, pos, whist + warp * R, tbl, bit, dmask);
           }
         }
         else if constexpr (STABLE)

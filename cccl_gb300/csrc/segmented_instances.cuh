@@ -61,6 +61,11 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
     gb300_seg_pass_k##KB##_v##VB##_##FS(const gb300::SegDeviceParams p)                                              \
   {                                                                                                                  \
     gb300::seg_device_onesweep_body<KB, VB, FP, gb300::seg_pass_tpb(KB, VB), gb300::seg_pass_items(KB, VB)>(p);      \
+  }                                                                                                                  \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_ppass_tpb(KB, VB), 1)                                     \
+    gb300_seg_ppass_k##KB##_v##VB##_##FS(const gb300::SegDeviceParams p)                                             \
+  {                                                                                                                  \
+    gb300::seg_device_persistent_body<KB, VB, FP, gb300::seg_ppass_tpb(KB, VB), gb300::seg_ppass_items(KB, VB)>(p);  \
   }
 
 #define GB300_SEG_HIST(KB, FP, FS)                                                                                   \

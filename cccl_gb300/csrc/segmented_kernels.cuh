@@ -769,3 +769,465 @@ __device__ __forceinline__ void seg_device_onesweep_body(const SegDeviceParams& 
 }
 
 } // namespace gb300
+
+namespace gb300
+{
+
+// ---------------------------------------------------------------------------------------
+// Device class, pipelined: the same digit pass over all large segments as
+// seg_device_onesweep_body, in the persistent, warp-specialised form of the plain pass
+// (onesweep_persistent_impl): one CTA per SM walks the global tile list blockIdx.x,
+// blockIdx.x + gridDim.x, ...; 256 look-back threads walk a tile's segment chain while the
+// main threads rank it, and a tile is written out one iteration later.
+//
+// Tiles start anywhere inside a segment, so a tile's keys (and values) rarely start on a
+// 16-byte boundary: the bulk copy fetches the 16-byte-aligned range that covers them (up to
+// 32 bytes more than the tile) and the tile is read from its offset inside the buffer. The
+// one tile whose covering range would reach past the end of the array is read with plain
+// loads. A tile's geometry (segment, index inside the segment, keys) is worked out by the
+// thread that issues its copy and kept beside its buffer.
+//
+// Forward progress: tile t waits only on lower tiles of its own segment, which are lower
+// global tiles, held by CTAs that are all resident (cooperative launch) and that take their
+// tiles in increasing order.
+// ---------------------------------------------------------------------------------------
+template <int KB, int VB, int TPB, int ITEMS>
+struct SegPersistentSmem
+{
+  using U                   = typename uint_of<KB>::type;
+  using V                   = typename value_word<VB>::type;
+  static constexpr int MT   = TPB - LOOKBACK_THREADS;
+  static constexpr int NW   = MT / 32;
+  static constexpr int TILE = MT * ITEMS;
+  static constexpr size_t whist_off  = 0;
+  static constexpr size_t gdelta_off = whist_off + sizeof(uint32_t) * NW * RADIX_DIGITS;
+  static constexpr size_t misc_off   = gdelta_off + sizeof(long long) * RADIX_DIGITS;
+  static constexpr size_t geo_off    = misc_off + 128; // 3 slots of SEG_GEO_WORDS words
+  static constexpr size_t buf_off    = geo_off + 256;
+  static constexpr size_t kbytes     = ((sizeof(U) * TILE + 15) / 16) * 16 + 32; // covering range
+  static constexpr size_t vbytes     = VB > 0 ? ((sizeof(V) * TILE + 15) / 16) * 16 + 32 : 0;
+  static constexpr size_t buf_bytes  = kbytes + vbytes;
+  static constexpr size_t bytes      = buf_off + 3 * buf_bytes;
+  static_assert(seg_persistent_smem_for(KB, VB, TPB, ITEMS) == bytes, "host and kernel layouts agree");
+};
+
+// geometry words of a tile slot
+enum : int
+{
+  SEG_GEO_LOCAL = 0, // tile index inside its segment
+  SEG_GEO_VALID,     // keys in the tile
+  SEG_GEO_BASE,      // global tile index of the segment's first tile (its first look-back row)
+  SEG_GEO_SEG,       // index into the device-class list
+  SEG_GEO_KOFF,      // first key's element offset in the buffer (bulk-copied tiles)
+  SEG_GEO_VOFF,
+  SEG_GEO_BULK,      // 1: fetched by bulk copy, 0: read with plain loads
+  SEG_GEO_BEGIN_LO,  // global index of the tile's first key
+  SEG_GEO_BEGIN_HI,
+  SEG_GEO_WORDS = 16
+};
+
+template <int KB, int VB, int FP, int TPB, int ITEMS>
+__device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams& dp)
+{
+  using L            = SegPersistentSmem<KB, VB, TPB, ITEMS>;
+  using U            = typename L::U;
+  using V            = typename L::V;
+  constexpr int MT   = L::MT;
+  constexpr int NW   = L::NW;
+  constexpr int R    = RADIX_DIGITS;
+  constexpr int TILE = L::TILE;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint32_t* whist   = reinterpret_cast<uint32_t*>(smem + L::whist_off);
+  long long* gdelta = reinterpret_cast<long long*>(smem + L::gdelta_off);
+  uint32_t* misc    = reinterpret_cast<uint32_t*>(smem + L::misc_off);
+  uint64_t* mbar    = reinterpret_cast<uint64_t*>(misc + 16);
+  uint32_t* geo     = reinterpret_cast<uint32_t*>(smem + L::geo_off);
+  auto kbuf         = [&](int b) {
+    return reinterpret_cast<U*>(smem + L::buf_off + size_t(b) * L::buf_bytes);
+  };
+  auto vbuf = [&](int b) {
+    return reinterpret_cast<V*>(smem + L::buf_off + size_t(b) * L::buf_bytes + L::kbytes);
+  };
+
+  const int tid         = threadIdx.x;
+  const int pass        = dp.pass;
+  const uint32_t ntiles = (*dp.status & STATUS_SEG_CAPACITY) ? 0u : dp.counters[SEG_CTR_DEVICE_TILES];
+  const U* keys_src     = static_cast<const U*>(dp.keys_src[pass]);
+  const V* values_src   = static_cast<const V*>(dp.values_src[pass]);
+  const int bit         = dp.pass_bit[pass];
+  const uint32_t dmask  = (1u << dp.pass_bits[pass]) - 1u;
+  const bool encode_in  = pass == 0;
+  const bool decode_out = pass == dp.num_passes - 1;
+  uint32_t* lookback      = dp.lookback[pass & 1];
+  uint32_t* lookback_next = (pass + 1 < dp.num_passes) ? dp.lookback[(pass + 1) & 1] : nullptr;
+
+  // thread 0: the geometry of tile t into slot b, and its bulk copy when it can have one
+  auto issue = [&](uint32_t t, int b) {
+    const uint32_t si       = dp.tile_segment[t];
+    const DeviceSegment seg = dp.device_list[si];
+    const uint32_t local    = t - seg.tile_base;
+    const uint32_t first    = local * uint32_t(TILE);
+    const uint32_t valid    = min(uint32_t(TILE), seg.size - first);
+    const unsigned long long begin = seg.begin + first;
+    uint32_t* g          = geo + b * SEG_GEO_WORDS;
+    g[SEG_GEO_LOCAL]     = local;
+    g[SEG_GEO_VALID]     = valid;
+    g[SEG_GEO_BASE]      = seg.tile_base;
+    g[SEG_GEO_SEG]       = si;
+    g[SEG_GEO_BEGIN_LO]  = uint32_t(begin);
+    g[SEG_GEO_BEGIN_HI]  = uint32_t(begin >> 32);
+    const uintptr_t ka   = reinterpret_cast<uintptr_t>(keys_src + begin);
+    const uintptr_t ka0  = ka & ~uintptr_t(15);
+    const uint32_t kb    = uint32_t(((ka + uintptr_t(valid) * KB + 15) & ~uintptr_t(15)) - ka0);
+    bool bulk            = ka0 + kb <= reinterpret_cast<uintptr_t>(keys_src + dp.num_items);
+    uintptr_t va = 0, va0 = 0;
+    uint32_t vb = 0;
+    if constexpr (VB > 0)
+    {
+      va   = reinterpret_cast<uintptr_t>(values_src + begin);
+      va0  = va & ~uintptr_t(15);
+      vb   = uint32_t(((va + uintptr_t(valid) * sizeof(V) + 15) & ~uintptr_t(15)) - va0);
+      bulk = bulk && va0 + vb <= reinterpret_cast<uintptr_t>(values_src + dp.num_items);
+    }
+    g[SEG_GEO_KOFF] = uint32_t(ka - ka0) / KB;
+    g[SEG_GEO_VOFF] = VB > 0 ? uint32_t(va - va0) / uint32_t(sizeof(V)) : 0u;
+    g[SEG_GEO_BULK] = bulk ? 1u : 0u;
+    if (bulk)
+    {
+      mbar_arrive_expect_tx(&mbar[b], kb + vb);
+      bulk_copy_g2s(kbuf(b), reinterpret_cast<const void*>(ka0), kb, &mbar[b]);
+      if constexpr (VB > 0)
+      {
+        bulk_copy_g2s(vbuf(b), reinterpret_cast<const void*>(va0), vb, &mbar[b]);
+      }
+    }
+  };
+
+  if (tid == 0)
+  {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    mbar_init(&mbar[2], 1);
+    mbar_init_fence();
+    misc[2] = 0u;
+    if (blockIdx.x < ntiles)
+    {
+      issue(blockIdx.x, 0);
+    }
+  }
+  for (int i = tid; i < NW * R; i += TPB)
+  {
+    whist[i] = 0;
+  }
+  __syncthreads();
+
+  if (tid < MT)
+  {
+    // ================================ main threads ================================
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+    const int wofs = warp * ITEMS * 32 + lane;
+    U* kout        = static_cast<U*>(dp.keys_dst[pass]);
+    V* vout        = static_cast<V*>(dp.values_dst[pass]);
+
+    // consecutive staging slots of one digit go to consecutive outputs; every store is
+    // bounds-checked against the array, so corrupted offsets cannot write outside it
+    auto write_out_as = [&](int b, uint32_t valid, auto decode_tag, auto narrow_tag) {
+      constexpr bool DECODE              = decltype(decode_tag)::value;
+      constexpr bool NARROW              = decltype(narrow_tag)::value;
+      const U* ks                        = kbuf(b);
+      const V* vs                        = vbuf(b);
+      const unsigned long long out_limit = misc[2] != 0u ? 0ull : dp.num_items;
+      const int32_t* gdelta32            = reinterpret_cast<const int32_t*>(gdelta);
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j)
+      {
+        const uint32_t s = j * MT + tid;
+        if (s < valid)
+        {
+          const U k        = ks[s];
+          const uint32_t d = extract_digit<U, FP>(k, bit, dmask);
+          const U out      = DECODE ? decode_key<U>(k, dp.codec) : k;
+          if constexpr (NARROW)
+          {
+            const uint32_t g = uint32_t(gdelta32[2 * d] + int32_t(s));
+            if (g < uint32_t(out_limit))
+            {
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vs[s]);
+              }
+            }
+          }
+          else
+          {
+            const long long g = gdelta[d] + (long long) s;
+            if ((unsigned long long) g < out_limit)
+            {
+              __stcs(kout + g, out);
+              if constexpr (VB > 0)
+              {
+                __stcs(vout + g, vs[s]);
+              }
+            }
+          }
+        }
+      }
+    };
+    auto write_out = [&](int b, uint32_t valid) {
+      const bool narrow = dp.num_items < (1ull << 31);
+      if (decode_out)
+      {
+        if (narrow)
+        {
+          write_out_as(b, valid, BoolTag<true>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out_as(b, valid, BoolTag<true>{}, BoolTag<false>{});
+        }
+      }
+      else
+      {
+        if (narrow)
+        {
+          write_out_as(b, valid, BoolTag<false>{}, BoolTag<true>{});
+        }
+        else
+        {
+          write_out_as(b, valid, BoolTag<false>{}, BoolTag<false>{});
+        }
+      }
+    };
+
+    uint32_t parity     = 0; // bit b: phase parity to wait for on buffer b
+    int buf             = 0;
+    int prev_buf        = 0;
+    uint32_t prev_valid = 0;
+    bool have_prev      = false;
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+    {
+      const uint32_t tn = t + gridDim.x;
+      const int nbuf    = buf == 2 ? 0 : buf + 1;
+      if (tid == 0 && tn < ntiles)
+      {
+        fence_proxy_async_smem(); // buffer nbuf was last accessed by the generic proxy
+        issue(tn, nbuf);
+      }
+
+      // ---- load (encode on the first pass; keys past the tile are all-ones: they rank last) ----
+      const uint32_t* g     = geo + buf * SEG_GEO_WORDS;
+      const uint32_t valid  = g[SEG_GEO_VALID];
+      U keys[ITEMS];
+      V vals[VB > 0 ? ITEMS : 1];
+      if (g[SEG_GEO_BULK] != 0u)
+      {
+        const bool data_ok = mbar_wait(&mbar[buf], (parity >> buf) & 1u);
+        parity ^= 1u << buf;
+        if (!data_ok)
+        {
+          // the copy never completed: this CTA stores nothing from here on
+          atomicOr(dp.status, STATUS_LOOKBACK_TIMEOUT);
+          misc[2] = 1u;
+        }
+        const U* ks = kbuf(buf) + g[SEG_GEO_KOFF];
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          const uint32_t idx = uint32_t(wofs + i * 32);
+          keys[i]            = idx < valid ? (encode_in ? encode_key<U>(ks[idx], dp.codec) : ks[idx]) : U(~U(0));
+        }
+        if constexpr (VB > 0)
+        {
+          const V* vs = vbuf(buf) + g[SEG_GEO_VOFF];
+#pragma unroll
+          for (int i = 0; i < ITEMS; ++i)
+          {
+            const uint32_t idx = uint32_t(wofs + i * 32);
+            if (idx < valid)
+            {
+              vals[i] = vs[idx];
+            }
+          }
+        }
+      }
+      else
+      {
+        const unsigned long long begin = (unsigned long long) g[SEG_GEO_BEGIN_LO] | ((unsigned long long) g[SEG_GEO_BEGIN_HI] << 32);
+        const U* kin                   = keys_src + begin;
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          const uint32_t idx = uint32_t(wofs + i * 32);
+          keys[i]            = idx < valid ? (encode_in ? encode_key<U>(kin[idx], dp.codec) : kin[idx]) : U(~U(0));
+        }
+        if constexpr (VB > 0)
+        {
+          const V* vin = values_src + begin;
+#pragma unroll
+          for (int i = 0; i < ITEMS; ++i)
+          {
+            const uint32_t idx = uint32_t(wofs + i * 32);
+            if (idx < valid)
+            {
+              vals[i] = __ldcs(vin + idx);
+            }
+          }
+        }
+      }
+      warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+      if (tid == 0)
+      {
+        misc[4] = extract_digit<U, FP>(keys[0], bit, dmask);
+      }
+      asm volatile("bar.arrive 3, %0;" ::"n"(TPB) : "memory"); // BH: counts of t ready
+
+      // ---- the previous tile goes out while the look-back threads turn t's counts into positions ----
+      if (have_prev)
+      {
+        asm volatile("bar.sync 5, %0;" ::"n"(TPB) : "memory"); // BG: offsets of the previous tile
+        write_out(prev_buf, prev_valid);
+      }
+      asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO: positions of t in whist
+
+      // ---- rank t, stage it in its own buffer (every main thread read it before BO) ----
+      const uint32_t single = misc[3];
+      uint32_t pos[ITEMS];
+      if (single != 0u)
+      {
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          pos[i] = uint32_t(wofs + i * 32);
+        }
+      }
+      else
+      {
+        __syncwarp();
+        warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+      }
+      U* ks = kbuf(buf);
+#pragma unroll
+      for (int i = 0; i < ITEMS; ++i)
+      {
+        ks[pos[i]] = keys[i];
+      }
+      if constexpr (VB > 0)
+      {
+        V* vs = vbuf(buf);
+#pragma unroll
+        for (int i = 0; i < ITEMS; ++i)
+        {
+          vs[pos[i]] = vals[i];
+        }
+      }
+      __syncwarp();
+      for (int k = lane; k < R; k += 32)
+      {
+        whist[warp * R + k] = 0u;
+      }
+      asm volatile("bar.sync 6, %0;" ::"n"(MT) : "memory");
+      prev_buf   = buf;
+      prev_valid = valid;
+      have_prev  = true;
+      buf        = nbuf;
+    }
+    if (have_prev)
+    {
+      asm volatile("bar.sync 5, %0;" ::"n"(TPB) : "memory"); // BG of the last tile
+      write_out(prev_buf, prev_valid);
+    }
+  }
+  else
+  {
+    // ============================== look-back threads ==============================
+    const int d              = tid - MT;
+    const uint32_t skip_tile = gb300_fault_skip_tile; // no tile, unless a test withholds one
+    int buf                  = 0;
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
+    {
+      asm volatile("bar.sync 3, %0;" ::"n"(TPB) : "memory"); // BH
+      const uint32_t* g       = geo + buf * SEG_GEO_WORDS;
+      const uint32_t valid    = g[SEG_GEO_VALID];
+      const uint32_t local    = g[SEG_GEO_LOCAL];
+      const uint32_t row_base = g[SEG_GEO_BASE];
+      const uint32_t si       = g[SEG_GEO_SEG];
+      buf                     = buf == 2 ? 0 : buf + 1;
+      uint32_t start;
+      const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start, d);
+      if (uint32_t(d) == misc[4])
+      {
+        // every real key of the tile has the first key's digit (padding keys, digit dmask,
+        // are discounted)
+        const uint32_t real = total - (uint32_t(d) == dmask ? uint32_t(TILE) - valid : 0u);
+        misc[3]             = real == valid ? (1u | (uint32_t(d) << 8)) : 0u;
+      }
+      uint32_t* col      = lookback + (size_t) row_base * R + d; // this segment's chain, digit d
+      const bool publish = t != skip_tile;
+      if (publish)
+      {
+        store_status(col + (size_t) local * R, (local == 0 ? LB_INCLUSIVE : LB_PARTIAL) | total);
+      }
+      asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO
+
+      uint32_t excl = 0;
+      if (local > 0)
+      {
+        bool failed = false;
+        bool done   = false;
+        for (int j = int(local) - 1; !done; j -= PERSISTENT_LOOKBACK_BATCH)
+        {
+          uint32_t w[PERSISTENT_LOOKBACK_BATCH];
+#pragma unroll
+          for (int k = 0; k < PERSISTENT_LOOKBACK_BATCH; ++k)
+          {
+            w[k] = (j - k >= 0) ? load_status(col + (size_t) (j - k) * R) : LB_INCLUSIVE;
+          }
+#pragma unroll
+          for (int k = 0; k < PERSISTENT_LOOKBACK_BATCH; ++k)
+          {
+            if (!done)
+            {
+              uint32_t v = w[k];
+              if ((v & LB_FLAGS) == LB_EMPTY)
+              {
+                v = wait_status(col + (size_t) (j - k) * R);
+              }
+              const uint32_t f = v & LB_FLAGS;
+              if (f == LB_ERROR)
+              {
+                failed = true;
+                done   = true;
+              }
+              else
+              {
+                excl += v & LB_VALUE;
+                done = (f == LB_INCLUSIVE);
+              }
+            }
+          }
+        }
+        if (publish)
+        {
+          store_status(col + (size_t) local * R, failed ? LB_ERROR : (LB_INCLUSIVE | (excl + total)));
+        }
+        if (failed)
+        {
+          atomicOr(dp.status, STATUS_LOOKBACK_TIMEOUT);
+          misc[2] = 1u;
+        }
+      }
+      if (lookback_next != nullptr)
+      {
+        lookback_next[(size_t) t * R + d] = 0u;
+      }
+      const unsigned long long base = dp.seg_bins[((size_t) si * dp.num_passes + pass) * R + d] + excl;
+      gdelta[d]                     = (long long) base - (long long) start;
+      asm volatile("bar.arrive 5, %0;" ::"n"(TPB) : "memory"); // BG
+    }
+  }
+}
+
+} // namespace gb300

@@ -46,7 +46,8 @@ void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&na
     "gb300_seg_scan",
     "gb300_seg_pass_" + rad,
     "gb300_seg_small_" + kv + "r" + fs,
-    "gb300_seg_medium_" + kv + "r" + fs};
+    "gb300_seg_medium_" + kv + "r" + fs,
+    "gb300_seg_ppass_" + rad};
   for (int i = 0; i < SK_COUNT; ++i)
   {
     std::snprintf(names[i], sizeof(names[i]), "%s", n[i].c_str());
@@ -76,6 +77,9 @@ SegmentedPolicy make_segmented_policy(int kb, int vb, int kind)
   p.block_s_smem        = seg_block_smem(kb, seg_block_s_tpb(kb), seg_block_s_items(kb));
   p.block_l_smem        = seg_block_smem(kb, seg_block_l_tpb(kb), seg_block_l_items(kb));
   p.pass_smem           = onesweep_smem_for(kb, vb, seg_pass_tpb(kb, vb), seg_pass_items(kb, vb));
+  p.ppass_tpb           = seg_ppass_tpb(kb, vb);
+  p.ppass_items         = seg_ppass_items(kb, vb);
+  p.ppass_smem          = seg_ppass_smem(kb, vb);
   return p;
 }
 
@@ -145,9 +149,19 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   }
 
   // ---- temporary storage ----
-  const uint64_t pass_tile = uint64_t(pol.pass_tpb) * pol.pass_items;
+  // The pipelined pass bulk-copies 16-byte-aligned ranges of the pass buffers, so it needs
+  // aligned buffers (the temporary ones are); otherwise the CTA-per-tile pass runs. The
+  // tile size follows the kernel.
+  auto aligned16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  const bool pipelined = aligned16(c.keys[0]) && aligned16(c.keys[1])
+                      && (!has_vals || (aligned16(c.values[0]) && aligned16(c.values[1])));
+  const uint64_t ptile     = uint64_t(pol.ppass_tpb - LOOKBACK_THREADS) * pol.ppass_items;
+  const uint64_t ctile     = uint64_t(pol.pass_tpb) * pol.pass_items;
+  const uint64_t pass_tile = pipelined ? ptile : ctile;
   const uint64_t max_dev   = std::min<uint64_t>(nseg, n / (uint64_t(pol.block_l_cap) + 1));
-  const uint64_t max_tiles = ceil_div(n, pass_tile) + max_dev;
+  // tile lists and look-back rows sized for the smaller tile of the two pass kernels, so the
+  // size a caller queried is enough whichever kernel the buffers' alignment selects
+  const uint64_t max_tiles = ceil_div(n, std::min(ptile, ctile)) + max_dev;
   const bool need_tmp      = !c.overwrite && passes > 1 && max_dev > 0;
 
   size_t off               = 0;
@@ -344,11 +358,24 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     }
     launch("seg_hist", ks.k[SK_HIST], unsigned(sms * 4), HISTOGRAM_TPB, 0, c.stream, p);
     launch("seg_scan", ks.k[SK_SCAN], unsigned(sms * 4), 256, 0, c.stream, p);
-    const unsigned pass_grid = unsigned(sms * occupancy(ks.k[SK_PASS], pol.pass_tpb, pol.pass_smem));
-    for (int q = 0; q < passes; ++q)
+    if (pipelined)
     {
-      p.pass = q;
-      launch("seg_pass", ks.k[SK_PASS], pass_grid, unsigned(pol.pass_tpb), pol.pass_smem, c.stream, p);
+      // persistent: every CTA resident (a tile waits on lower tiles of its segment)
+      const unsigned grid = unsigned(sms * occupancy(ks.k[SK_PPASS], pol.ppass_tpb, pol.ppass_smem));
+      for (int q = 0; q < passes; ++q)
+      {
+        p.pass = q;
+        launch_cooperative("seg_pass", ks.k[SK_PPASS], grid, unsigned(pol.ppass_tpb), pol.ppass_smem, c.stream, p);
+      }
+    }
+    else
+    {
+      const unsigned pass_grid = unsigned(sms * occupancy(ks.k[SK_PASS], pol.pass_tpb, pol.pass_smem));
+      for (int q = 0; q < passes; ++q)
+      {
+        p.pass = q;
+        launch("seg_pass", ks.k[SK_PASS], pass_grid, unsigned(pol.pass_tpb), pol.pass_smem, c.stream, p);
+      }
     }
   }
   *selector = target;

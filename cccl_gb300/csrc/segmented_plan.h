@@ -36,6 +36,9 @@ struct SegmentedPolicy
   uint64_t block_s_smem;
   uint64_t block_l_smem;
   uint64_t pass_smem;
+  int32_t ppass_tpb; // pipelined device-class pass (buffers 16-byte aligned)
+  int32_t ppass_items;
+  uint64_t ppass_smem;
 };
 
 SegmentedPolicy make_segmented_policy(int key_bytes, int value_bytes, int key_kind);
@@ -54,6 +57,7 @@ enum SegKernel : int
   SK_PASS,
   SK_RSMALL,  // the networks in radix order (segmented radix sort, learned buckets)
   SK_RMEDIUM,
+  SK_PPASS,   // the pipelined device-class pass
   SK_COUNT
 };
 

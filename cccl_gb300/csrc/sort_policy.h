@@ -339,6 +339,39 @@ GB300_HD constexpr int seg_pass_items(int kb, int vb)
   return (void) kb, (void) vb, 8;
 #endif
 }
+
+// Pipelined device-class pass (seg_device_persistent_body): the persistent pass's threads,
+// and as many items as three tile buffers with 32 bytes of alignment slack each (keys and
+// values) leave room for.
+GB300_HD constexpr int seg_ppass_tpb(int kb, int vb)
+{
+  return persistent_tpb(kb, vb);
+}
+GB300_HD constexpr size_t seg_persistent_smem_for(int kb, int vb, int tpb, int items)
+{
+  return size_t(4) * ((tpb - LOOKBACK_THREADS) / 32) * 256 + size_t(8) * 256 + 128 + 256
+       + 3 * (round16(size_t(kb) * (tpb - LOOKBACK_THREADS) * items) + 32
+              + (vb > 0 ? round16(value_word_bytes(vb) * (tpb - LOOKBACK_THREADS) * items) + 32 : 0));
+}
+GB300_HD constexpr int seg_ppass_items(int kb, int vb)
+{
+  // 4-byte keys: capped where the plain pass's item counts spilled registers here (the tile
+  // geometry and the offset reads take a few more)
+#ifdef GB300_SEG_PPASS_ITEMS
+  int items = GB300_SEG_PPASS_ITEMS;
+#else
+  int items = kb == 4 ? (vb == 0 ? 12 : vb == 4 ? 11 : persistent_items_nominal(kb, vb)) : persistent_items_nominal(kb, vb);
+#endif
+  while (items > 1 && seg_persistent_smem_for(kb, vb, seg_ppass_tpb(kb, vb), items) > size_t(227) * 1024)
+  {
+    --items;
+  }
+  return items;
+}
+GB300_HD constexpr size_t seg_ppass_smem(int kb, int vb)
+{
+  return seg_persistent_smem_for(kb, vb, seg_ppass_tpb(kb, vb), seg_ppass_items(kb, vb));
+}
 } // namespace gb300
 
 namespace gb300
