@@ -50,6 +50,7 @@ HOST_SOURCES = [
     "learned_plan.cpp",
     "learned_sort_abi.cpp",
     "status_abi.cpp",
+    "value_gather.cpp",
 ]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]

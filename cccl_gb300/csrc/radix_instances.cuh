@@ -4,6 +4,7 @@
 #pragma once
 
 #include "radix_kernels.cuh"
+#include "gather_kernels.cuh"
 #include "sort_policy.h"
 
 #define GB300_CAT_(a, b) a##b

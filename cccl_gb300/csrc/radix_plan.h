@@ -28,7 +28,8 @@ struct RadixPolicy
   int32_t histogram_tpb;
   int32_t persistent_tpb;
   int32_t persistent_items;
-  int32_t reserved[5];
+  int32_t gather_value_bytes; // > 0: the caller's values have this width, sorted as 32-bit indices
+  int32_t reserved[4];
   uint64_t onesweep_smem;
   uint64_t single_tile_smem;
   uint64_t persistent_smem;

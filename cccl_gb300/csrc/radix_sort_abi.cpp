@@ -14,6 +14,7 @@
 
 #include "abi_common.h"
 #include "radix_plan.h"
+#include "value_gather.h"
 #include "sort_policy.h"
 
 using namespace gb300;
@@ -116,12 +117,15 @@ try
     return CUDA_ERROR_NOT_SUPPORTED;
   }
   const bool keys_only    = is_keys_only(input_values_it);
-  const size_t value_size = keys_only ? 0 : input_values_it.value_type.size;
-  if (!supported_value_bytes(value_size))
+  const size_t user_value = keys_only ? 0 : input_values_it.value_type.size;
+  if (!keys_only && (user_value == 0 || user_value > (size_t(1) << 20)))
   {
-    printf("\nERROR in cccl_device_radix_sort_compile(): value size %zu is not supported\n", value_size);
+    printf("\nERROR in cccl_device_radix_sort_compile(): value size %zu is not supported\n", user_value);
     return CUDA_ERROR_NOT_SUPPORTED;
   }
+  // widths the kernels do not carry travel as 32-bit indices and are gathered afterwards
+  const bool gathered     = !supported_value_bytes(user_value);
+  const size_t value_size = gathered ? 4 : user_value;
 
   const image_ref img = radix_image(key_bytes);
   std::unique_ptr<char[]> payload(new char[img.size]);
@@ -133,7 +137,8 @@ try
     return CUDA_ERROR_OUT_OF_MEMORY;
   }
   *pol = make_radix_policy(key_bytes, int(value_size), kind);
-  pol->magic = POLICY_MAGIC;
+  pol->magic              = POLICY_MAGIC;
+  pol->gather_value_bytes = gathered ? int32_t(user_value) : 0;
 
   const RadixKernelNames names = radix_kernel_names(key_bytes, int(value_size), kind, sort_order == CCCL_DESCENDING);
   const std::string& one   = names.onesweep;
@@ -355,7 +360,25 @@ CCCL_C_API CUresult cccl_device_radix_sort(
     call.temp_storage_bytes = temp_storage_bytes;
     call.stream           = stream;
     int sel               = 0;
-    radix_sort_dispatch(pol, ks, call, &sel);
+    if (pol.gather_value_bytes > 0 && call.values[0] != nullptr)
+    {
+      sort_with_gathered_values(
+        build.library, uint32_t(pol.gather_value_bytes), call.values, num_items, is_overwrite_okay, false,
+        d_temp_storage, temp_storage_bytes, stream,
+        [&](void* const idx[2], void* temp, size_t* bytes, int* s) {
+          RadixCall inner      = call;
+          inner.values[0]      = idx[0];
+          inner.values[1]      = idx[1];
+          inner.d_temp_storage = temp;
+          inner.temp_storage_bytes = bytes;
+          radix_sort_dispatch(pol, ks, inner, s);
+        },
+        &sel);
+    }
+    else
+    {
+      radix_sort_dispatch(pol, ks, call, &sel);
+    }
     *selector = sel;
     return CUDA_SUCCESS;
   }

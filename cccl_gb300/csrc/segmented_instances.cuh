@@ -3,6 +3,7 @@
 #pragma once
 
 #include "segmented_kernels.cuh"
+#include "gather_kernels.cuh"
 #include "sort_policy.h"
 
 extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitParams p)

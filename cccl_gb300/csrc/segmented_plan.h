@@ -39,6 +39,8 @@ struct SegmentedPolicy
   int32_t ppass_tpb; // pipelined device-class pass (buffers 16-byte aligned)
   int32_t ppass_items;
   uint64_t ppass_smem;
+  int32_t gather_value_bytes; // > 0: the caller's values have this width, sorted as 32-bit indices
+  int32_t pad0;
 };
 
 SegmentedPolicy make_segmented_policy(int key_bytes, int value_bytes, int key_kind);

@@ -12,6 +12,7 @@
 
 #include "abi_common.h"
 #include "segmented_plan.h"
+#include "value_gather.h"
 #include "sort_policy.h"
 
 using namespace gb300;
@@ -138,7 +139,25 @@ CUresult segmented_run(const char* who,
     call.begin_bit          = begin_bit;
     call.end_bit            = end_bit;
     int sel                 = 0;
-    segmented_sort_dispatch(pol, ks, call, &sel);
+    if (pol.gather_value_bytes > 0 && call.values[0] != nullptr)
+    {
+      sort_with_gathered_values(
+        build.library, uint32_t(pol.gather_value_bytes), call.values, num_items, is_overwrite_okay, true,
+        d_temp_storage, temp_storage_bytes, stream,
+        [&](void* const idx[2], void* temp, size_t* bytes, int* s) {
+          SegmentedCall inner      = call;
+          inner.values[0]          = idx[0];
+          inner.values[1]          = idx[1];
+          inner.d_temp_storage     = temp;
+          inner.temp_storage_bytes = bytes;
+          segmented_sort_dispatch(pol, ks, inner, s);
+        },
+        &sel);
+    }
+    else
+    {
+      segmented_sort_dispatch(pol, ks, call, &sel);
+    }
     *selector = sel;
     return CUDA_SUCCESS;
   }
@@ -185,12 +204,16 @@ try
     printf("\nERROR in cccl_device_segmented_sort_compile(): unsupported key type\n");
     return CUDA_ERROR_NOT_SUPPORTED;
   }
-  const size_t vb = keys_only(d_values_in) ? 0 : d_values_in.value_type.size;
-  if (!(vb == 0 || vb == 4 || vb == 8))
+  const size_t user_value = keys_only(d_values_in) ? 0 : d_values_in.value_type.size;
+  if (!keys_only(d_values_in) && (user_value == 0 || user_value > (size_t(1) << 20)))
   {
-    printf("\nERROR in cccl_device_segmented_sort_compile(): value size %zu is not supported (0, 4 or 8)\n", vb);
+    printf("\nERROR in cccl_device_segmented_sort_compile(): value size %zu is not supported\n", user_value);
     return CUDA_ERROR_NOT_SUPPORTED;
   }
+  // the kernels carry 4- and 8-byte values; other widths (custom types) travel as 32-bit
+  // indices and are gathered afterwards
+  const bool gathered = !(user_value == 0 || user_value == 4 || user_value == 8);
+  const size_t vb     = gathered ? 4 : user_value;
   const image_ref img = segmented_image(kb);
   std::unique_ptr<char[]> payload(new char[img.size]);
   std::memcpy(payload.get(), img.data, img.size);
@@ -205,6 +228,7 @@ try
   }
   *pol       = make_segmented_policy(kb, int(vb), kind);
   pol->magic = SEG_POLICY_MAGIC;
+  pol->gather_value_bytes = gathered ? int32_t(user_value) : 0;
   tab->magic = SEG_TABLE_MAGIC;
   segmented_kernel_names(kb, int(vb), kind, sort_order == CCCL_DESCENDING, tab->names);
 

@@ -78,6 +78,25 @@ struct StatusFoldParams
   uint32_t pad0;
 };
 
+// Values of widths the kernels do not carry: sorted as 32-bit indices, then gathered.
+constexpr uint32_t VALUES_SKIP = 0xffffffffu; // index of a position the sort did not write
+
+struct ValuesIotaParams
+{
+  uint32_t* out;
+  unsigned long long n;
+};
+
+struct ValuesGatherParams
+{
+  const void* src;
+  void* dst;
+  const uint32_t* idx;
+  unsigned long long n;
+  uint32_t width; // bytes per value
+  uint32_t word;  // bytes per copy: divides width and both buffers' alignment
+};
+
 struct InitParams
 {
   uint32_t* words;

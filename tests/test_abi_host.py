@@ -101,8 +101,13 @@ def test_compile_rejections(lib):
     assert _compile(lib, cc=(9, 0))[0] == B.CUDA_ERROR_NOT_SUPPORTED
     assert _compile(lib, decomposer_name=b"my_decomposer")[0] == B.CUDA_ERROR_NOT_SUPPORTED
     assert _compile(lib, key_type=(B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
-    assert _compile(lib, value_type=(B.STORAGE, 12))[0] == B.CUDA_ERROR_NOT_SUPPORTED
     assert _compile(lib, value_type=(B.STORAGE, 16))[0] == B.CUDA_SUCCESS
+    # values of other widths (custom structs) are accepted: the kernels carry 32-bit indices
+    # (the build's kernels are the 4-byte-value ones) and the run gathers the values
+    rc, b = _compile(lib, value_type=(B.STORAGE, 12))
+    assert rc == B.CUDA_SUCCESS and b.onesweep_kernel_lowered_name.endswith(b"_v4_i")
+    assert lib.cccl_device_radix_sort_cleanup(C.byref(b)) == B.CUDA_SUCCESS
+    assert _compile(lib, value_type=(B.STORAGE, 0))[0] == B.CUDA_ERROR_NOT_SUPPORTED
     assert lib.cccl_device_radix_sort_cleanup(None) == B.CUDA_ERROR_INVALID_VALUE
     assert lib.cccl_device_radix_sort_load(None) == B.CUDA_ERROR_INVALID_VALUE
 
