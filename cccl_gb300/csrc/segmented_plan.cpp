@@ -47,7 +47,8 @@ void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&na
     "gb300_seg_pass_" + rad,
     "gb300_seg_small_" + kv + "r" + fs,
     "gb300_seg_medium_" + kv + "r" + fs,
-    "gb300_seg_ppass_" + rad};
+    "gb300_seg_ppass_" + rad,
+    "gb300_seg_hist_lanes_k" + std::to_string(kb) + "_" + fs};
   for (int i = 0; i < SK_COUNT; ++i)
   {
     std::snprintf(names[i], sizeof(names[i]), "%s", n[i].c_str());
@@ -356,7 +357,16 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
       p.keys_src[q]   = q == 0 ? c.keys[0] : p.keys_dst[q - 1];
       p.values_src[q] = has_vals ? (q == 0 ? c.values[0] : p.values_dst[q - 1]) : nullptr;
     }
-    launch("seg_hist", ks.k[SK_HIST], unsigned(sms * 4), HISTOGRAM_TPB, 0, c.stream, p);
+    if (passes <= 8)
+    {
+      // one lane-column CTA per SM over a contiguous range of the tile list
+      launch("seg_hist", ks.k[SK_HIST_LANES], unsigned(sms), HISTOGRAM_LANES_TPB, histogram_table_bytes(passes),
+             c.stream, p);
+    }
+    else
+    {
+      launch("seg_hist", ks.k[SK_HIST], unsigned(sms * 4), HISTOGRAM_TPB, 0, c.stream, p);
+    }
     launch("seg_scan", ks.k[SK_SCAN], unsigned(sms * 4), 256, 0, c.stream, p);
     if (pipelined)
     {
