@@ -1,7 +1,7 @@
 """Autotuner of the kernel shapes on the GPU it runs on.
 
 The shapes (threads per CTA, keys per thread, CTAs per SM the registers are sized for, the
-block classes' algorithm) are compile-time constants of the kernels, chosen per key and value
+block classes' algorithm and digit bits) are compile-time constants of the kernels, chosen per key and value
 width by the table in ``cccl_gb300/csrc/sort_policy.h``. The tuner rebuilds the library once
 per candidate with ``GB300_TUNE_DEFINES`` (the overrides that table honours), times the
 affected kernels on synthetic inputs through the launch observer, and writes every
@@ -14,7 +14,9 @@ at the end.
 
 Groups:
   onesweep  persistent onesweep pass (plain sort): u64+u32 pairs, f32+u32 pairs, u32 keys
+  sizes     the persistent pass's items per thread per size class: 2^20, 2^24, 2^28 keys
   block     segmented block classes: ~4096-key segments, f32+i32 and f64+i64
+  blockbits digit bits of the block classes' passes (5 to 8), per key type and class
   segpass   segmented device-class pass: lognormal segments, f32+i32 and f64+i64
   writeout  the pass write-out with and without 32-bit positions (the onesweep group's cases)
 """
@@ -50,6 +52,20 @@ CANDIDATES = {
     "writeout": [
         "",
         "-DGB300_WRITE_OUT_SPECIALISED=0",
+    ],
+    # digit bits of the block classes' in-shared-memory passes (block_s and block_l vary
+    # together; each class's time depends on its own bits only)
+    "blockbits": [
+        "",
+        "-DGB300_SEG_BLOCK_S_BITS=7 -DGB300_SEG_BLOCK_L_BITS=7",
+        "-DGB300_SEG_BLOCK_S_BITS=6 -DGB300_SEG_BLOCK_L_BITS=6",
+        "-DGB300_SEG_BLOCK_S_BITS=5 -DGB300_SEG_BLOCK_L_BITS=5",
+    ],
+    # persistent pass tile per size class: the pass time at 2^20, 2^24 and 2^28 keys
+    "sizes": [
+        "",
+        "-DGB300_PERSISTENT_ITEMS=7",
+        "-DGB300_PERSISTENT_ITEMS=4",
     ],
     "segpass": [
         "",
@@ -115,7 +131,15 @@ def measure(group):
         f = torch.randn(n, device="cuda", dtype=torch.float32)
         s = bench.Sorter(torch, f, with_values=True)
         out["f32+u32"] = _kernel_ms(torch, s.run, "onesweep")
-    elif group == "block":
+    elif group == "sizes":
+        for lg in (20, 24, 28):
+            n = 1 << lg
+            for name, dtype, pairs in (("u32 keys", "u32", False), ("u64+u32", "u64", True)):
+                s = bench.Sorter(torch, bench.make_inputs(torch, n, dtype), with_values=pairs)
+                out[f"{name} 2^{lg}"] = _kernel_ms(torch, s.run, "onesweep")
+                del s
+                torch.cuda.empty_cache()
+    elif group in ("block", "blockbits"):
         rng = np.random.default_rng(5)
         sizes_l = rng.integers(3000, 5200, size=(1 << 25) // 4100)  # block_l
         sizes_s = rng.integers(300, 2048, size=(1 << 24) // 1200)  # block_s

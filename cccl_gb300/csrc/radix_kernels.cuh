@@ -449,7 +449,7 @@ struct SingleTileSmem
 // Reads keys_in/values_in, writes keys_out/values_out (which may alias the inputs: all
 // reads complete before the first write). Starts with a CTA barrier so a persistent CTA
 // can call it for one segment after another.
-template <int KB, int VB, int FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS, int BITS = RADIX_BITS>
 __device__ __forceinline__ void block_sort_body(
   const void* keys_in,
   void* keys_out,
@@ -465,8 +465,8 @@ __device__ __forceinline__ void block_sort_body(
   using V            = typename value_word<VB>::type;
   constexpr int NW   = L::NW;
   constexpr int TILE = L::TILE;
-  constexpr int R    = RADIX_DIGITS;
-  static_assert(TPB >= R, "the digit-parallel phases need one thread per digit");
+  constexpr int R    = 1 << BITS; // digits of one in-shared-memory pass
+  static_assert(TPB >= R && BITS >= 5 && BITS <= RADIX_BITS, "one thread per digit, whole warps of digits");
   static_assert(TILE <= 65536, "16-bit source indices");
 
   extern __shared__ __align__(128) unsigned char smem[];
@@ -536,9 +536,9 @@ __device__ __forceinline__ void block_sort_body(
   const int active_warps = int((n + ITEMS * 32 - 1) / (ITEMS * 32));
 
   int cur = 0;
-  for (int bit = lo_bit; bit < hi_bit; bit += RADIX_BITS)
+  for (int bit = lo_bit; bit < hi_bit; bit += BITS)
   {
-    const uint32_t dmask = (1u << min(RADIX_BITS, hi_bit - bit)) - 1u;
+    const uint32_t dmask = (1u << min(BITS, hi_bit - bit)) - 1u;
     for (int i = tid; i < NW * R; i += TPB)
     {
       whist[i] = 0;
@@ -566,14 +566,14 @@ __device__ __forceinline__ void block_sort_body(
     if (tid < R)
     {
       uint32_t tstart;
-      block_digit_offsets<NW>(whist, misc + 8, &tstart);
+      block_digit_offsets<NW, R>(whist, misc + 8, &tstart);
     }
     __syncthreads();
     if (active)
     {
       uint32_t pos[ITEMS];
       __syncwarp(); // the warp votes below need a converged warp
-      warp_rank_stable<U, FP, ITEMS>(keys, pos, whist + warp * R, bit, dmask);
+      warp_rank_stable<U, FP, ITEMS, BITS>(keys, pos, whist + warp * R, bit, dmask);
 #pragma unroll
       for (int i = 0; i < ITEMS; ++i)
       {

@@ -49,13 +49,15 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
   extern "C" __global__ void __launch_bounds__(gb300::seg_block_s_tpb(KB), gb300::seg_block_minb(KB))              \
     gb300_seg_block_s_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                             \
   {                                                                                                                  \
-    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_s_tpb(KB), gb300::seg_block_s_items(KB)>(                     \
+    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_s_tpb(KB), gb300::seg_block_s_items(KB),               \
+                          gb300::seg_block_s_bits(KB)>(                                                            \
       p, p.block_s_list, gb300::SEG_CTR_BLOCK_S, gb300::SEG_CTR_TICKET_BLOCK_S);                                     \
   }                                                                                                                  \
   extern "C" __global__ void __launch_bounds__(gb300::seg_block_l_tpb(KB), gb300::seg_block_minb(KB))              \
     gb300_seg_block_l_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                             \
   {                                                                                                                  \
-    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)>(                     \
+    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB),               \
+                          gb300::seg_block_l_bits(KB)>(                                                            \
       p, p.block_l_list, gb300::SEG_CTR_BLOCK_L, gb300::SEG_CTR_TICKET_BLOCK_L);                                     \
   }                                                                                                                  \
   extern "C" __global__ void __launch_bounds__(gb300::seg_pass_tpb(KB, VB))                                         \

@@ -545,7 +545,7 @@ __device__ __forceinline__ void seg_network_body(const SegSortParams& p, const u
 // ---------------------------------------------------------------------------------------
 // block class: one CTA per segment, shared-memory LSD passes
 // ---------------------------------------------------------------------------------------
-template <int KB, int VB, int FP, int TPB, int ITEMS>
+template <int KB, int VB, int FP, int TPB, int ITEMS, int BITS = RADIX_BITS>
 __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uint32_t* list, uint32_t count_index,
                                                uint32_t ticket_index)
 {
@@ -581,7 +581,7 @@ __device__ __forceinline__ void seg_block_body(const SegSortParams& p, const uin
     }
     else
     {
-      block_sort_body<KB, VB, FP, TPB, ITEMS>(static_cast<const U*>(p.keys_in) + b,
+      block_sort_body<KB, VB, FP, TPB, ITEMS, BITS>(static_cast<const U*>(p.keys_in) + b,
                                               static_cast<U*>(p.keys_out) + b,
                                               VB > 0 ? static_cast<const V*>(p.values_in) + b : nullptr,
                                               VB > 0 ? static_cast<V*>(p.values_out) + b : nullptr,

@@ -309,6 +309,25 @@ GB300_HD constexpr int seg_block_l_items(int kb)
   return seg_block_algo(kb) == SEG_BLOCK_MERGE || kb == 8 ? 8 : 16;
 #endif
 }
+// Digit bits of one in-shared-memory radix pass of the block classes (5 to 8): fewer bits
+// cost fewer ballots per key and smaller counter rows, more passes. Picked per key width and
+// class by the autotuner (cccl_gb300/tuning_gb300.json, group "blockbits").
+GB300_HD constexpr int seg_block_s_bits(int kb)
+{
+#ifdef GB300_SEG_BLOCK_S_BITS
+  return (void) kb, GB300_SEG_BLOCK_S_BITS;
+#else
+  return (void) kb, 8;
+#endif
+}
+GB300_HD constexpr int seg_block_l_bits(int kb)
+{
+#ifdef GB300_SEG_BLOCK_L_BITS
+  return (void) kb, GB300_SEG_BLOCK_L_BITS;
+#else
+  return (void) kb, 8;
+#endif
+}
 GB300_HD constexpr int seg_block_s_tpb(int kb)
 {
   return SEG_BLOCK_S_CAP / seg_block_s_items(kb);

@@ -33,11 +33,14 @@ __device__ __forceinline__ uint32_t lanemask_le()
   return m;
 }
 
-// Exclusive prefix over the 256 digit slots held by one group of 256 threads (eight whole
-// warps; thread d holds digit d's value). `scratch` holds 8 words. Must be called by
-// exactly that group, and by no other thread of the CTA at the same time (named barrier 1).
+// Exclusive prefix over the R digit slots held by one group of R threads (R / 32 whole
+// warps; thread d holds digit d's value; R = 256 for 8-bit digits). `scratch` holds 8 words.
+// Must be called by exactly that group, and by no other thread of the CTA at the same time
+// (named barrier 1).
+template <int R = RADIX_DIGITS>
 __device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* scratch, int d = threadIdx.x)
 {
+  static_assert(R % 32 == 0 && R <= 256, "whole warps, at most 8");
   const int lane = d & 31;
   const int w    = d >> 5;
   uint32_t x     = v;
@@ -54,10 +57,10 @@ __device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* s
   {
     scratch[w] = x;
   }
-  named_barrier_256();
+  asm volatile("bar.sync 1, %0;" ::"n"(R) : "memory");
   uint32_t pre = 0;
 #pragma unroll
-  for (int j = 0; j < 8; ++j)
+  for (int j = 0; j < R / 32; ++j)
   {
     pre += (j < w) ? scratch[j] : 0u;
   }
@@ -67,11 +70,12 @@ __device__ __forceinline__ uint32_t digit_exclusive_scan(uint32_t v, uint32_t* s
 // Lanes whose 8-bit digit equals this lane's: one ballot per bit. Written in PTX so each
 // bit costs a bit test into a predicate, the vote, a predicated inversion and an AND
 // (measured 1.6x faster on GB300 than the select-based C++ form).
+template <int BITS = RADIX_BITS>
 __device__ __forceinline__ uint32_t warp_match_digit(uint32_t d)
 {
   uint32_t peers = 0xffffffffu;
 #pragma unroll
-  for (int b = 0; b < RADIX_BITS; ++b)
+  for (int b = 0; b < BITS; ++b)
   {
     uint32_t bal;
     asm("{\n"
@@ -99,10 +103,11 @@ __device__ __forceinline__ void warp_histogram(const U (&keys)[ITEMS], uint32_t*
   }
 }
 
-// One group of 256 threads (thread d, digit d): turns per-warp counts whist[w][d] into
-// tile positions (exclusive over digits, then over warps). Returns this thread's digit
-// total; *tile_start receives the digit's first position in the tile.
-template <int NW>
+// One group of R threads (thread d, digit d; R = 256 for 8-bit digits): turns per-warp
+// counts whist[w][d] (rows of R) into tile positions (exclusive over digits, then over
+// warps). Returns this thread's digit total; *tile_start receives the digit's first position
+// in the tile.
+template <int NW, int R = RADIX_DIGITS>
 __device__ __forceinline__ uint32_t
 block_digit_offsets(uint32_t* whist, uint32_t* scratch8, uint32_t* tile_start, int d = threadIdx.x)
 {
@@ -110,22 +115,23 @@ block_digit_offsets(uint32_t* whist, uint32_t* scratch8, uint32_t* tile_start, i
 #pragma unroll
   for (int w = 0; w < NW; ++w)
   {
-    const uint32_t c        = whist[w * RADIX_DIGITS + d];
-    whist[w * RADIX_DIGITS + d] = total;
+    const uint32_t c = whist[w * R + d];
+    whist[w * R + d] = total;
     total += c;
   }
-  const uint32_t start = digit_exclusive_scan(total, scratch8, d);
+  const uint32_t start = digit_exclusive_scan<R>(total, scratch8, d);
 #pragma unroll
   for (int w = 0; w < NW; ++w)
   {
-    whist[w * RADIX_DIGITS + d] += start;
+    whist[w * R + d] += start;
   }
   *tile_start = start;
   return total;
 }
 
 // Stable tile positions: pos[i] = whist_w[d] at the time key i is reached, in source order.
-template <class U, int FP, int ITEMS>
+// Digits have BITS bits (8 in the digit passes).
+template <class U, int FP, int ITEMS, int BITS = RADIX_BITS>
 __device__ __forceinline__ void warp_rank_stable(
   const U (&keys)[ITEMS], uint32_t (&pos)[ITEMS], uint32_t* whist_w, int bit, uint32_t dmask)
 {
@@ -135,7 +141,7 @@ __device__ __forceinline__ void warp_rank_stable(
   for (int i = 0; i < ITEMS; ++i)
   {
     const uint32_t d      = extract_digit<U, FP>(keys[i], bit, dmask);
-    const uint32_t peers  = warp_match_digit(d);
+    const uint32_t peers  = warp_match_digit<BITS>(d);
     const int leader      = 31 - __clz(peers);
     const uint32_t cnt_le = __popc(peers & le);
     uint32_t base         = 0;
