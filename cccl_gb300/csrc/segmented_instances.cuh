@@ -76,11 +76,6 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
     gb300_seg_hist_k##KB##_##FS(const gb300::SegDeviceParams p)                                                      \
   {                                                                                                                  \
     gb300::seg_device_histogram_body<KB, FP, gb300::HISTOGRAM_TPB>(p);                                               \
-  }                                                                                                                  \
-  extern "C" __global__ void __launch_bounds__(gb300::HISTOGRAM_LANES_TPB, 1)                                       \
-    gb300_seg_hist_lanes_k##KB##_##FS(const gb300::SegDeviceParams p)                                                \
-  {                                                                                                                  \
-    gb300::seg_device_histogram_lanes_body<KB, FP, gb300::HISTOGRAM_LANES_TPB>(p);                                   \
   }
 
 // radix-order networks: KIND = NET_RADIX + FP mode, their own shapes

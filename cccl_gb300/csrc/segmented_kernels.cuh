@@ -1231,137 +1231,3 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
 }
 
 } // namespace gb300
-
-namespace gb300
-{
-
-// ---------------------------------------------------------------------------------------
-// Per-segment digit counts with lane-column counters (the plain sort's histogram layout,
-// histogram_lanes_body): every lane owns a column of counters per (pass, digit), so a
-// warp's 32 reduction-adds hit 32 banks (16 shared columns for passes 4-7). One CTA of 1024
-// threads per SM takes a contiguous range of the device-class tile list and keeps counting
-// while the tiles stay in one segment; when the segment changes, every row of columns is
-// summed by a warp, added to that segment's counts and cleared. Digits may be any width
-// (the split pass that fixes the buffer parity has fewer than 8 bits), so the counter
-// address is computed with a multiply-add instead of a byte permute. Up to 8 passes.
-// ---------------------------------------------------------------------------------------
-template <int KB, int FP, int TPB>
-__device__ __forceinline__ void seg_device_histogram_lanes_body(const SegDeviceParams& p)
-{
-  using U         = typename uint_of<KB>::type;
-  constexpr int R = RADIX_DIGITS;
-  extern __shared__ __align__(16) unsigned char table[];
-  const uint32_t ntiles = (*p.status & STATUS_SEG_CAPACITY) ? 0u : p.counters[SEG_CTR_DEVICE_TILES];
-  const int tid         = threadIdx.x;
-  const int lane        = tid & 31;
-  const int warp        = tid >> 5;
-  const int P           = p.num_passes; // <= 8 (the host launches the CTA-table kernel otherwise)
-
-  for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < (unsigned long long) ntiles * R;
-       i += (unsigned long long) gridDim.x * TPB)
-  {
-    p.lookback[0][i] = 0u;
-  }
-  const uint32_t table_bytes = uint32_t(histogram_table_bytes(P));
-  for (uint32_t i = uint32_t(tid) * 16u; i < table_bytes; i += uint32_t(TPB) * 16u)
-  {
-    *reinterpret_cast<uint4*>(table + i) = make_uint4(0u, 0u, 0u, 0u);
-  }
-  uint32_t col[8]; // byte 0 and byte 2 of this lane's counter offsets, per pass
-  uint32_t shift[8];
-  uint32_t mask[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q)
-  {
-    col[q]   = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(q & 1) * 128u + uint32_t(lane) * 4u))
-                     : ((2u << 16) | (uint32_t(q & 3) * 64u + uint32_t(lane & 15) * 4u));
-    shift[q] = q < P ? uint32_t(p.pass_bit[q]) : 0u;
-    mask[q]  = q < P ? (1u << p.pass_bits[q]) - 1u : 0u;
-  }
-  const uint32_t table_base = smem_addr(table);
-
-  // sums every row of columns into segment si's counts and clears the table
-  auto flush = [&](uint32_t si) {
-    __syncthreads();
-    for (int r = warp; r < P * R; r += TPB / 32)
-    {
-      const int q          = r >> 8;
-      const int d          = r & (R - 1);
-      const int width      = q < 4 ? 32 : 16;
-      const uint32_t base  = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(d) << 8) | (uint32_t(q & 1) * 128u))
-                                   : ((2u << 16) | (uint32_t(d) << 8) | (uint32_t(q & 3) * 64u));
-      uint32_t* w          = reinterpret_cast<uint32_t*>(table + base + 4u * uint32_t(lane));
-      const uint32_t x     = lane < width ? *w : 0u;
-      const uint32_t total = __reduce_add_sync(0xffffffffu, x);
-      if (lane < width)
-      {
-        *w = 0u;
-      }
-      if (lane == 0 && total != 0u)
-      {
-        atomicAdd(&p.seg_counts[(size_t) si * P * R + r], total);
-      }
-    }
-    __syncthreads();
-  };
-
-  const uint32_t t0 = uint32_t((unsigned long long) ntiles * blockIdx.x / gridDim.x);
-  const uint32_t t1 = uint32_t((unsigned long long) ntiles * (blockIdx.x + 1) / gridDim.x);
-  uint32_t cur      = 0xffffffffu;
-  __syncthreads();
-  for (uint32_t t = t0; t < t1; ++t)
-  {
-    const uint32_t si = p.tile_segment[t];
-    if (si != cur)
-    {
-      if (cur != 0xffffffffu)
-      {
-        flush(cur);
-      }
-      cur = si;
-    }
-    const DeviceSegment seg = p.device_list[si];
-    const uint32_t first    = (t - seg.tile_base) * p.device_tile;
-    const uint32_t valid    = min(p.device_tile, seg.size - first);
-    const U* keys           = static_cast<const U*>(p.keys_in) + seg.begin + first;
-    auto count = [&](U raw) {
-      const U k = digit_source<U, FP>(encode_key<U>(raw, p.codec));
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-      {
-        if (q < P)
-        {
-          const uint32_t d   = uint32_t(k >> shift[q]) & mask[q];
-          const uint32_t off = d * 256u + col[q];
-          asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(table_base + off));
-        }
-      }
-    };
-    // four loads in flight per thread
-    uint32_t i = uint32_t(tid);
-    for (; i + 3u * TPB < valid; i += 4u * TPB)
-    {
-      U k[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-      {
-        k[j] = __ldcs(keys + i + j * TPB);
-      }
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-      {
-        count(k[j]);
-      }
-    }
-    for (; i < valid; i += TPB)
-    {
-      count(keys[i]);
-    }
-  }
-  if (cur != 0xffffffffu)
-  {
-    flush(cur);
-  }
-}
-
-} // namespace gb300

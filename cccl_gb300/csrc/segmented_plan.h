@@ -60,7 +60,6 @@ enum SegKernel : int
   SK_RSMALL,  // the networks in radix order (segmented radix sort, learned buckets)
   SK_RMEDIUM,
   SK_PPASS,   // the pipelined device-class pass
-  SK_HIST_LANES, // the lane-column per-segment histogram (up to 8 passes)
   SK_COUNT
 };
 

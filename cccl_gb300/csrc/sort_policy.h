@@ -311,7 +311,10 @@ GB300_HD constexpr int seg_block_l_items(int kb)
 }
 // Digit bits of one in-shared-memory radix pass of the block classes (5 to 8): fewer bits
 // cost fewer ballots per key and smaller counter rows, more passes. Picked per key width and
-// class by the autotuner (cccl_gb300/tuning_gb300.json, group "blockbits").
+// class by the autotuner (cccl_gb300/tuning_gb300.json, group "blockbits"); measured on
+// GB300 (block_s / block_l time), 8 / 7 / 6 / 5 bits: f32+i32 0.328 / 0.332 / 0.345 / 0.425
+// and 0.676 / 0.708 / 0.751 / 0.869 ms; f64+i64 0.856 / 0.908 / 0.922 / 1.006 and 1.664 /
+// 1.812 / 1.853 / 2.078 ms. Eight bits win for both widths and both classes.
 GB300_HD constexpr int seg_block_s_bits(int kb)
 {
 #ifdef GB300_SEG_BLOCK_S_BITS
@@ -499,6 +502,12 @@ GB300_HD constexpr size_t learned_bucket_smem(int kb, int vb, int cap)
 // that needs no more partition passes than 4096-key buckets, else 4096.
 GB300_HD constexpr int learned_bucket_items_log2(int log2n)
 {
+#ifdef GB300_LEARNED_ITEMS_LOG2
+  if (GB300_LEARNED_ITEMS_LOG2 == 11 || GB300_LEARNED_ITEMS_LOG2 == 12)
+  {
+    return GB300_LEARNED_ITEMS_LOG2; // tuning builds
+  }
+#endif
   const int b11 = log2n - 11 < 8 ? 8 : (log2n - 11 > LEARNED_MAX_BUCKET_LOG2 ? LEARNED_MAX_BUCKET_LOG2 : log2n - 11);
   const int b12 = log2n - 12 < 8 ? 8 : (log2n - 12 > LEARNED_MAX_BUCKET_LOG2 ? LEARNED_MAX_BUCKET_LOG2 : log2n - 12);
   return (b11 + 7) / 8 == (b12 + 7) / 8 ? 11 : 12;
