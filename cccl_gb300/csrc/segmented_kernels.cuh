@@ -637,15 +637,34 @@ __device__ __forceinline__ void seg_device_histogram_body(const SegDeviceParams&
     const uint32_t first     = local * p.device_tile;
     const uint32_t valid     = min(p.device_tile, seg.size - first);
     const U* keys            = static_cast<const U*>(p.keys_in) + seg.begin + first;
-    for (uint32_t i = tid; i < valid; i += TPB)
-    {
-      const U k = encode_key<U>(keys[i], p.codec);
+    const uint32_t sh_base   = smem_addr(sh);
+    auto count_key           = [&](U raw) {
+      const U k = encode_key<U>(raw, p.codec);
       for (int q = 0; q < p.num_passes; ++q)
       {
-        const int b  = p.pass_bit[q];
-        const int nb = p.pass_bits[q];
-        atomicAdd(&sh[q * R + extract_digit<U, FP>(k, b, (1u << nb) - 1u)], 1u);
+        const uint32_t d = extract_digit<U, FP>(k, p.pass_bit[q], (1u << p.pass_bits[q]) - 1u);
+        asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(sh_base + 4u * uint32_t(q * R + int(d))));
       }
+    };
+    // four loads in flight per thread
+    uint32_t i = tid;
+    for (; i + 3u * TPB < valid; i += 4u * TPB)
+    {
+      U k[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        k[j] = __ldcs(keys + i + j * TPB);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        count_key(k[j]);
+      }
+    }
+    for (; i < valid; i += TPB)
+    {
+      count_key(keys[i]);
     }
     __syncthreads();
     for (int i = tid; i < p.num_passes * R; i += TPB)
