@@ -16,6 +16,7 @@ LIB_PATH = _PKG / "_build" / "libccclsort.so"
 INT8, INT16, INT32, INT64, UINT8, UINT16, UINT32, UINT64 = range(8)
 FLOAT16, FLOAT32, FLOAT64, STORAGE, BOOLEAN = 8, 9, 10, 11, 12
 POINTER, ITERATOR = 0, 1  # cccl_iterator_kind_t
+OP_LTOIR, OP_CPP_SOURCE = 0, 1  # cccl_op_code_type
 ASCENDING, DESCENDING = 0, 1  # cccl_sort_order_t
 PAYLOAD_LTOIR, PAYLOAD_CUBIN = 0, 1
 
@@ -23,6 +24,7 @@ CUDA_SUCCESS = 0
 CUDA_ERROR_INVALID_VALUE = 1
 CUDA_ERROR_NOT_INITIALIZED = 3
 CUDA_ERROR_NOT_SUPPORTED = 801
+CUDA_ERROR_INVALID_SOURCE = 300
 CUDA_ERROR_UNKNOWN = 999
 
 
@@ -334,6 +336,34 @@ def pointer_iterator(ptr: int, type_enum: int, size: int, alignment: int | None 
     it.type = POINTER
     it.value_type = TypeInfo(size, alignment or size, type_enum)
     it.state = ptr or None
+    return it
+
+
+def code_iterator(state: bytes, alignment: int, type_enum: int, size: int, advance: tuple, dereference: tuple,
+                  code_type: int = OP_CPP_SOURCE) -> Iterator:
+    """A CCCL_ITERATOR whose operations are given as code (the reference's calling convention:
+    ``extern "C" __device__ void advance(void* state, const void* diff)`` with a 64-bit
+    unsigned ``diff``, ``extern "C" __device__ void dereference(const void* state, T* out)``).
+    ``advance`` and ``dereference`` are ``(name, code)`` pairs, ``code`` C++ source or LTO-IR
+    bytes. ``state`` holds the iterator's state bytes; the returned object keeps every buffer
+    it points to alive."""
+    it = Iterator()
+    it.size = len(state)
+    it.alignment = alignment
+    it.type = ITERATOR
+    it.value_type = TypeInfo(size, size, type_enum)
+    keep = [C.create_string_buffer(bytes(state), len(state))]
+    it.state = C.cast(keep[0], C.c_void_p)
+    for field, (name, code) in (("advance", advance), ("dereference", dereference)):
+        op = Op()
+        op.type = 0  # CCCL_STATELESS
+        keep += [name.encode() if isinstance(name, str) else name, code.encode() if isinstance(code, str) else code]
+        op.name = keep[-2]
+        op.code = keep[-1]
+        op.code_size = len(keep[-1])
+        op.code_type = code_type
+        setattr(it, field, op)
+    it._keep = keep
     return it
 
 

@@ -51,6 +51,7 @@ HOST_SOURCES = [
     "learned_sort_abi.cpp",
     "status_abi.cpp",
     "value_gather.cpp",
+    "offset_iterators.cpp",
 ]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]

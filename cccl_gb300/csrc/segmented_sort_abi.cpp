@@ -11,6 +11,7 @@
 #include <memory>
 
 #include "abi_common.h"
+#include "offset_iterators.h"
 #include "segmented_plan.h"
 #include "value_gather.h"
 #include "sort_policy.h"
@@ -31,7 +32,21 @@ struct SegKernelTable
   uint32_t magic;
   char names[SK_COUNT][64];
   CUkernel handles[SK_COUNT];
+  // begin and end offsets given as iterators: their evaluation kernels, compiled at build
+  // time (null: both are pointers; an entry without an image is a pointer)
+  OffsetIteratorKernel* offsets;
 };
+
+void free_offsets(SegKernelTable* tab)
+{
+  if (tab != nullptr && tab->offsets != nullptr)
+  {
+    free_offset_iterator(tab->offsets[0]);
+    free_offset_iterator(tab->offsets[1]);
+    delete[] tab->offsets;
+    tab->offsets = nullptr;
+  }
+}
 
 bool keys_only(const cccl_iterator_t& values)
 {
@@ -44,6 +59,7 @@ void free_result(cccl_device_segmented_sort_build_result_t* b)
   b->payload = nullptr;
   std::free(b->runtime_policy);
   b->runtime_policy = nullptr;
+  free_offsets(static_cast<SegKernelTable*>(b->partition_runtime_policy));
   std::free(b->partition_runtime_policy);
   b->partition_runtime_policy = nullptr;
   for (char** p :
@@ -93,9 +109,15 @@ CUresult segmented_run(const char* who,
     fflush(stdout);
     return CUDA_ERROR_UNKNOWN;
   }
-  if (start_offset_in.type != CCCL_POINTER || end_offset_in.type != CCCL_POINTER)
+  const bool iter_begin = start_offset_in.type == CCCL_ITERATOR;
+  const bool iter_end   = end_offset_in.type == CCCL_ITERATOR;
+  if ((iter_begin || iter_end)
+      && (build.partition_runtime_policy == nullptr
+          || static_cast<const SegKernelTable*>(build.partition_runtime_policy)->offsets == nullptr
+          || (iter_begin && static_cast<const SegKernelTable*>(build.partition_runtime_policy)->offsets[0].kernel == nullptr)
+          || (iter_end && static_cast<const SegKernelTable*>(build.partition_runtime_policy)->offsets[1].kernel == nullptr)))
   {
-    printf("\nERROR in %s(): segment offsets must be pointers\n", who);
+    printf("\nERROR in %s(): segment offsets are iterators, but the build compiled pointer offsets\n", who);
     return CUDA_ERROR_NOT_SUPPORTED;
   }
   const size_t osz = start_offset_in.value_type.size;
@@ -120,19 +142,53 @@ CUresult segmented_run(const char* who,
       ks.k[i] = tab.handles[i];
     }
     SegmentedCall call{};
+    // offsets given as iterators are evaluated, in their own type, into arrays at the tail
+    // of the temporary storage (the sort's own part, with its status word, stays at the
+    // front); the sort reads those like pointers
+    const int n_iter       = int(iter_begin) + int(iter_end);
+    const size_t off_bytes = n_iter > 0 ? align_up(size_t(num_segments) * osz, 16) : 0;
+    const size_t tail      = n_iter * off_bytes;
+    const bool sizing      = d_temp_storage == nullptr;
+    if (!sizing && *temp_storage_bytes < tail)
+    {
+      throw cuda_error(CUDA_ERROR_INVALID_VALUE, "temp storage is smaller than the size query returned");
+    }
+    auto* tbase        = static_cast<unsigned char*>(d_temp_storage);
+    size_t inner_bytes = sizing ? 0 : (*temp_storage_bytes - tail) / 16 * 16;
+    void* offsets[2]   = {start_offset_in.state, end_offset_in.state};
+    for (int e = 0, slot = 0; e < 2; ++e)
+    {
+      const cccl_iterator_t& oit = e == 0 ? start_offset_in : end_offset_in;
+      if (oit.type != CCCL_ITERATOR)
+      {
+        continue;
+      }
+      // placeholders while sizing: aligned and non-null, never read
+      offsets[e] = sizing ? reinterpret_cast<void*>(uintptr_t(256) * (e + 1))
+                          : static_cast<void*>(tbase + inner_bytes + slot * off_bytes);
+      if (!sizing)
+      {
+        if (tab.offsets[e].value_size != osz)
+        {
+          throw cuda_error(CUDA_ERROR_INVALID_VALUE, "offset iterator type differs from the one the build compiled");
+        }
+        evaluate_offset_iterator(tab.offsets[e], oit, num_segments, offsets[e], stream);
+      }
+      ++slot;
+    }
     call.keys[0]            = d_keys_in.state;
     call.keys[1]            = d_keys_out.state;
     call.values[0]          = d_values_in.state;
     call.values[1]          = d_values_out.state;
     call.num_items          = num_items;
     call.num_segments       = num_segments;
-    call.begin_offsets      = start_offset_in.state;
-    call.end_offsets        = end_offset_in.state;
+    call.begin_offsets      = offsets[0];
+    call.end_offsets        = offsets[1];
     call.offsets_64         = osz == 8 ? 1 : 0;
     call.overwrite          = is_overwrite_okay;
     call.descending         = build.order == CCCL_DESCENDING;
     call.d_temp_storage     = d_temp_storage;
-    call.temp_storage_bytes = temp_storage_bytes;
+    call.temp_storage_bytes = n_iter == 0 ? temp_storage_bytes : &inner_bytes;
     call.stream             = stream;
     call.target             = -1;
     call.radix_only         = radix_only;
@@ -143,7 +199,7 @@ CUresult segmented_run(const char* who,
     {
       sort_with_gathered_values(
         build.library, uint32_t(pol.gather_value_bytes), call.values, num_items, is_overwrite_okay, true,
-        d_temp_storage, temp_storage_bytes, stream,
+        call.d_temp_storage, call.temp_storage_bytes, stream,
         [&](void* const idx[2], void* temp, size_t* bytes, int* s) {
           SegmentedCall inner      = call;
           inner.values[0]          = idx[0];
@@ -157,6 +213,10 @@ CUresult segmented_run(const char* who,
     else
     {
       segmented_sort_dispatch(pol, ks, call, &sel);
+    }
+    if (n_iter > 0 && sizing)
+    {
+      *temp_storage_bytes = align_up(inner_bytes, 16) + tail;
     }
     *selector = sel;
     return CUDA_SUCCESS;
@@ -177,7 +237,7 @@ CCCL_C_API CUresult cccl_device_segmented_sort_compile(
   cccl_iterator_t d_keys_in,
   cccl_iterator_t d_values_in,
   cccl_iterator_t begin_offset_in,
-  cccl_iterator_t /*end_offset_in*/,
+  cccl_iterator_t end_offset_in,
   int cc_major,
   int cc_minor,
   const char*,
@@ -231,6 +291,28 @@ try
   pol->gather_value_bytes = gathered ? int32_t(user_value) : 0;
   tab->magic = SEG_TABLE_MAGIC;
   segmented_kernel_names(kb, int(vb), kind, sort_order == CCCL_DESCENDING, tab->names);
+  if (begin_offset_in.type == CCCL_ITERATOR || end_offset_in.type == CCCL_ITERATOR)
+  {
+    try
+    {
+      tab->offsets = new OffsetIteratorKernel[2]{};
+      if (begin_offset_in.type == CCCL_ITERATOR)
+      {
+        compile_offset_iterator(begin_offset_in, &end_offset_in, cc_major, cc_minor, tab->offsets[0]);
+      }
+      if (end_offset_in.type == CCCL_ITERATOR)
+      {
+        compile_offset_iterator(end_offset_in, &begin_offset_in, cc_major, cc_minor, tab->offsets[1]);
+      }
+    }
+    catch (...)
+    {
+      free_offsets(tab);
+      std::free(pol);
+      std::free(tab);
+      throw;
+    }
+  }
 
   cccl_device_segmented_sort_build_result_t r{};
   r.cc                            = cc_major * 10 + cc_minor;
@@ -279,9 +361,26 @@ try
     {
       check(cuLibraryGetKernel(&tab->handles[i], build->library, tab->names[i]), tab->names[i]);
     }
+    if (tab->offsets != nullptr)
+    {
+      load_offset_iterator(tab->offsets[0]);
+      load_offset_iterator(tab->offsets[1]);
+    }
   }
   catch (...)
   {
+    if (tab->offsets != nullptr)
+    {
+      for (int e = 0; e < 2; ++e)
+      {
+        if (tab->offsets[e].library != nullptr)
+        {
+          cuLibraryUnload(tab->offsets[e].library);
+          tab->offsets[e].library = nullptr;
+          tab->offsets[e].kernel  = nullptr;
+        }
+      }
+    }
     cuLibraryUnload(build->library);
     build->library = nullptr;
     throw;
@@ -445,6 +544,8 @@ try
   {
     h = nullptr; // handles belong to a loaded library; never serialized
   }
+  const OffsetIteratorKernel* offs = tab.offsets;
+  tab.offsets                      = nullptr;
   blob_writer w;
   write_header(w, ALGO_SEGMENTED, b->payload_kind, b->cc);
   w.type_info(b->key_type);
@@ -458,6 +559,15 @@ try
   w.cstr(b->segmented_sort_kernel_large_lowered_name);
   w.cstr(b->three_way_partition_init_kernel_lowered_name);
   w.cstr(b->three_way_partition_kernel_lowered_name);
+  // offset iterators: their evaluation images and state layouts
+  w.pod<uint32_t>(offs != nullptr ? 2u : 0u);
+  for (int e = 0; offs != nullptr && e < 2; ++e)
+  {
+    w.blob(offs[e].cubin, offs[e].cubin_size);
+    w.pod<uint64_t>(offs[e].state_size);
+    w.pod<uint64_t>(offs[e].state_alignment);
+    w.pod<uint64_t>(offs[e].value_size);
+  }
   w.release(out_buf, out_size);
   return CUDA_SUCCESS;
 }
@@ -514,10 +624,57 @@ try
   {
     name[sizeof(name) - 1] = '\0';
   }
-  std::unique_ptr<char[]> names[5];
-  for (auto& n : names)
+  for (auto& hd : tab->handles)
   {
-    n.reset(rd.cstr_new());
+    hd = nullptr;
+  }
+  tab->offsets = nullptr;
+  std::unique_ptr<char[]> names[5];
+  try
+  {
+    for (auto& n : names)
+    {
+      n.reset(rd.cstr_new());
+    }
+    const uint32_t n_offsets = rd.pod<uint32_t>();
+    if (n_offsets != 0 && n_offsets != 2)
+    {
+      throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: bad offset iterator count");
+    }
+    if (n_offsets == 2)
+    {
+      tab->offsets = new OffsetIteratorKernel[2]{};
+      for (int e = 0; e < 2; ++e)
+      {
+        size_t bytes = 0;
+        std::unique_ptr<char[]> img(static_cast<char*>(rd.blob_new(&bytes)));
+        OffsetIteratorKernel& k = tab->offsets[e];
+        k.state_size            = rd.pod<uint64_t>();
+        k.state_alignment       = rd.pod<uint64_t>();
+        k.value_size            = rd.pod<uint64_t>();
+        if (bytes > 0)
+        {
+          if (k.state_size == 0 || k.state_size > MAX_OFFSET_STATE_BYTES || (k.value_size != 4 && k.value_size != 8))
+          {
+            throw cuda_error(CUDA_ERROR_INVALID_VALUE, "serialization blob: bad offset iterator");
+          }
+          k.cubin = std::malloc(bytes);
+          if (k.cubin == nullptr)
+          {
+            throw cuda_error(CUDA_ERROR_OUT_OF_MEMORY, "offset iterator image");
+          }
+          std::memcpy(k.cubin, img.get(), bytes);
+          k.cubin_size = bytes;
+        }
+      }
+    }
+  }
+  catch (...)
+  {
+    free_offsets(tab);
+    std::free(pol);
+    std::free(tab);
+    throw;
   }
   r.payload                                      = payload.release();
   r.runtime_policy                               = pol;

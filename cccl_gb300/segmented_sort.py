@@ -28,7 +28,13 @@ from .radix_sort import (
 )
 
 
-def _offset_iterator(t: torch.Tensor) -> B.Iterator:
+def _offset_iterator(t) -> B.Iterator:
+    """A device array of int32/int64 offsets, or an iterator given as code
+    (``_bindings.code_iterator``), which the build compiles into an evaluation kernel."""
+    if isinstance(t, B.Iterator):
+        if t.type != B.ITERATOR or t.value_type.size not in (4, 8):
+            raise TypeError("segment offset iterators must yield int32 or int64")
+        return t
     _check_device_array(t, "segment offsets")
     if t.dtype not in (torch.int32, torch.int64):
         raise TypeError("segment offsets must be int32 or int64")

@@ -31,3 +31,41 @@ def edge_segments(sizes, gap=0):
         e.append(pos + s)
         pos += s + gap
     return np.array(b, dtype=np.int64), np.array(e, dtype=np.int64), pos
+
+
+def strided_offset_iterator(B, start: int, step: int, type_enum=None, size=8, prefix="seg", with_code=True):
+    """Offsets start + i * step, as the reference's tests build them from C++ source: a state
+    struct, an advance that adds the difference to an index and a dereference that scales it."""
+    import struct
+
+    type_enum = B.INT64 if type_enum is None else type_enum
+    ctype = {4: "int", 8: "long long"}[size]
+    state_src = f"struct {prefix}_state {{ long long index; long long step; }};\n"
+    adv = (f"{prefix}_advance", state_src + f"""
+extern "C" __device__ void {prefix}_advance(void* s, const void* d)
+{{
+  static_cast<{prefix}_state*>(s)->index += *static_cast<const unsigned long long*>(d);
+}}
+""")
+    der = (f"{prefix}_dereference", state_src + f"""
+extern "C" __device__ void {prefix}_dereference(const void* s, {ctype}* out)
+{{
+  const {prefix}_state* st = static_cast<const {prefix}_state*>(s);
+  *out = ({ctype}) (st->index * st->step);
+}}
+""")
+    if not with_code:  # operations named only: their code comes from the other offset iterator
+        adv, der = (adv[0], ""), (der[0], "")
+    return B.code_iterator(struct.pack("<qq", start // step if step else 0, step), 8, type_enum, size, adv, der)
+
+
+def nvrtc_available():
+    import ctypes as C
+
+    for n in ("libnvrtc.so.13", "/usr/local/cuda/lib64/libnvrtc.so.13"):
+        try:
+            C.CDLL(n)
+            return True
+        except OSError:
+            pass
+    return False

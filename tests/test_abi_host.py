@@ -246,3 +246,69 @@ def test_segmented_run_rejections(lib, entry):
     assert call(o=bad) == B.CUDA_ERROR_NOT_SUPPORTED  # offsets through iterators
     assert call(o=narrow, e=narrow) == B.CUDA_ERROR_INVALID_VALUE  # 16-bit offsets
     lib.cccl_device_segmented_sort_cleanup(C.byref(b))
+
+
+# ---- segment offsets given as iterators (compiled at build time with NVRTC + nvJitLink) ----
+from segments import nvrtc_available as _nvrtc_available, strided_offset_iterator  # noqa: E402
+
+@pytest.mark.skipif(not _nvrtc_available(), reason="NVRTC is not installed")
+@pytest.mark.parametrize("osize", [4, 8])
+def test_segmented_compile_with_offset_iterators(lib, osize):
+    from cccl_gb300 import _bindings as B
+
+    otype = B.INT32 if osize == 4 else B.INT64
+    begin = strided_offset_iterator(B, 0, 100, otype, osize, "b")
+    end = strided_offset_iterator(B, 100, 100, otype, osize, "e")
+    keys = B.pointer_iterator(0x1000, B.UINT32, 4)
+    vals = B.pointer_iterator(0, B.STORAGE, 4)
+    b = B.SegmentedSortBuildResult()
+    rc = lib.cccl_device_segmented_sort_compile(C.byref(b), 0, keys, vals, begin, end, 10, 3, None, None, None, None,
+                                                None)
+    assert rc == B.CUDA_SUCCESS
+    # the evaluation images travel with a serialized build
+    buf, size = C.c_void_p(), C.c_size_t()
+    assert lib.cccl_device_segmented_sort_serialize(C.byref(b), C.byref(buf), C.byref(size)) == 0
+    plain_rc, plain = _seg_compile(lib, (B.UINT32, 4), offset_type=(otype, osize))
+    pbuf, psize = C.c_void_p(), C.c_size_t()
+    assert lib.cccl_device_segmented_sort_serialize(C.byref(plain), C.byref(pbuf), C.byref(psize)) == 0
+    assert size.value > psize.value + 2 * 1000  # two linked cubins
+    b2 = B.SegmentedSortBuildResult()
+    assert lib.cccl_device_segmented_sort_deserialize(C.byref(b2), buf, size) == 0
+    # a truncated blob is rejected without leaking the images read so far
+    b3 = B.SegmentedSortBuildResult()
+    assert lib.cccl_device_segmented_sort_deserialize(C.byref(b3), buf, size.value - 8) == B.CUDA_ERROR_INVALID_VALUE
+    for x in (buf, pbuf):
+        lib.cccl_serialization_buffer_free(x)
+    for x in (b, b2, plain):
+        assert lib.cccl_device_segmented_sort_cleanup(C.byref(x)) == 0
+
+
+@pytest.mark.skipif(not _nvrtc_available(), reason="NVRTC is not installed")
+def test_segmented_offset_iterator_rejections(lib):
+    from cccl_gb300 import _bindings as B
+
+    keys = B.pointer_iterator(0x1000, B.UINT32, 4)
+    vals = B.pointer_iterator(0, B.STORAGE, 4)
+    off = B.pointer_iterator(0x3000, B.INT64, 8)
+
+    def compile_with(begin, end=off):
+        b = B.SegmentedSortBuildResult()
+        rc = lib.cccl_device_segmented_sort_compile(C.byref(b), 0, keys, vals, begin, end, 10, 3, None, None, None,
+                                                    None, None)
+        if rc == 0:
+            lib.cccl_device_segmented_sort_cleanup(C.byref(b))
+        return rc
+
+    good = strided_offset_iterator(B, 0, 8)
+    assert compile_with(good) == B.CUDA_SUCCESS  # an iterator beside a pointer
+    broken = strided_offset_iterator(B, 0, 8)
+    broken.dereference.code = b"this is not C++"
+    broken.dereference.code_size = len(broken.dereference.code)
+    broken._keep.append(broken.dereference.code)
+    assert compile_with(broken) == B.CUDA_ERROR_INVALID_SOURCE
+    assert compile_with(strided_offset_iterator(B, 0, 8, B.INT16, 2) if False else
+                        B.code_iterator(b"\0" * 8, 8, B.FLOAT64, 8, ("a", "x"), ("d", "y"))) == B.CUDA_ERROR_NOT_SUPPORTED
+    unnamed = strided_offset_iterator(B, 0, 8)
+    unnamed.advance.name = b"bad name"
+    unnamed._keep.append(unnamed.advance.name)
+    assert compile_with(unnamed) == B.CUDA_ERROR_INVALID_VALUE

@@ -155,3 +155,75 @@ def test_segmented_radix_sort(oracle, bits, desc, overwrite):
         # DoubleBuffer: nothing runs (dispatch_segmented_radix_sort.cuh:541)
         expect = 0 if window[0] == window[1] else max(-(-(window[1] - window[0]) // 6), 1) % 2
         assert sel == expect
+
+
+@pytest.mark.parametrize("osize", [4, 8])
+@pytest.mark.parametrize("seg_size", [1000, 70_000])
+def test_offsets_through_iterators(oracle, osize, seg_size):
+    """Segment offsets given as iterators compiled from C++ source, the form the reference's
+    test sketches with its step-counting iterator (c/parallel/test/test_segmented_sort.cpp:
+    230-268): begin = i * size, end = (i + 1) * size, the end iterator naming the begin
+    iterator's operations without code. Results equal the pointer-offset sort's."""
+    import torch
+    from segments import nvrtc_available, strided_offset_iterator
+
+    import cccl_gb300 as cg
+    from cccl_gb300 import _bindings as B
+
+    if not nvrtc_available():
+        pytest.skip("NVRTC is not installed")
+    rng = np.random.default_rng(seg_size + osize)
+    nseg = max(4, 4_000_000 // seg_size)
+    n = nseg * seg_size
+    k = _nan_keys(np.float32, n, rng)
+    v = I.index_values(n)
+    otype = B.INT32 if osize == 4 else B.INT64
+    begin = strided_offset_iterator(B, 0, seg_size, otype, osize, "off")
+    end = strided_offset_iterator(B, seg_size, seg_size, otype, osize, "off", with_code=False)
+    dk = torch.from_numpy(k).cuda()
+    dv = torch.from_numpy(v).cuda()
+    ok = torch.empty_like(dk)
+    ov = torch.empty_like(dv)
+    cg.segmented_sort(d_in_keys=dk, d_out_keys=ok, d_in_values=dv, d_out_values=ov, num_items=n,
+                      num_segments=nseg, start_offsets_in=begin, end_offsets_in=end,
+                      order=cg.SortOrder.ASCENDING)
+    torch.cuda.synchronize()
+    b = np.arange(nseg, dtype=np.int64) * seg_size
+    rk, rv = oracle.segmented_sort(k, v, b, b + seg_size, descending=False, threads=8)
+    assert ok.cpu().numpy().tobytes() == rk.tobytes(), "keys differ from the oracle"
+    assert ov.cpu().numpy().tobytes() == rv.tobytes(), "values differ from the oracle"
+
+
+def test_iterator_beside_pointer_offsets(oracle):
+    """Begin offsets as a device array, end offsets as an iterator (and the build reused with
+    both as arrays)."""
+    import torch
+    from segments import nvrtc_available, strided_offset_iterator
+
+    import cccl_gb300 as cg
+    from cccl_gb300 import _bindings as B
+
+    if not nvrtc_available():
+        pytest.skip("NVRTC is not installed")
+    rng = np.random.default_rng(99)
+    seg, nseg = 333, 3000
+    n = seg * nseg
+    k = rng.integers(0, 2**32, n, dtype=np.uint32)
+    b = np.arange(nseg, dtype=np.int64) * seg
+    db = torch.from_numpy(b).cuda()
+    de = torch.from_numpy(b + seg).cuda()
+    end = strided_offset_iterator(B, seg, seg, B.INT64, 8, "endit")
+    dk = torch.from_numpy(k.view(np.int32)).cuda()
+    ok = torch.empty_like(dk)
+    sorter = cg.make_segmented_sort(d_in_keys=dk, d_out_keys=ok, start_offsets_in=db, end_offsets_in=end,
+                                    order=cg.SortOrder.DESCENDING)
+    rk, _ = oracle.segmented_sort(k.view(np.int32), None, b, b + seg, descending=True, threads=8)
+    for e_arg in (end, de):
+        ok.zero_()
+        nbytes = sorter(temp_storage=None, d_in_keys=dk, d_out_keys=ok, d_in_values=None, d_out_values=None,
+                        num_items=n, num_segments=nseg, start_offsets_in=db, end_offsets_in=e_arg)
+        tmp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device="cuda")
+        sorter(temp_storage=tmp, d_in_keys=dk, d_out_keys=ok, d_in_values=None, d_out_values=None, num_items=n,
+               num_segments=nseg, start_offsets_in=db, end_offsets_in=e_arg)
+        torch.cuda.synchronize()
+        assert ok.cpu().numpy().tobytes() == rk.tobytes()
