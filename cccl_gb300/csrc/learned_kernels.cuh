@@ -640,7 +640,10 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
         }
       }
     }
-    for (uint32_t i = tid; i < nb; i += TPB)
+    // at least 4 bins, so that the scan below works on whole 16-byte groups (the extra bins
+    // stay empty: no key maps to them)
+    const uint32_t nb4 = nb > 4u ? nb : 4u;
+    for (uint32_t i = tid; i < nb4; i += TPB)
     {
       bins[i] = 0u;
     }
@@ -711,17 +714,21 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
         }
       }
       __syncthreads();
-      // longest run; exclusive scan of the bins (thread t owns bins [t*per, (t+1)*per))
-      const uint32_t per   = (nb + TPB - 1) / TPB;
-      const uint32_t first = tid * per;
+      // longest run; exclusive scan of the bins. Thread t owns the 16-byte groups
+      // [t*gper, (t+1)*gper) of 4 bins each, read and written as uint4: scalar accesses at a
+      // stride of `per` words put 4 to 8 lanes on one bank.
+      const uint32_t groups = nb4 / 4u;
+      const uint32_t gper   = (groups + TPB - 1) / TPB;
+      const uint32_t first  = tid * gper;
+      uint4* bins4          = reinterpret_cast<uint4*>(bins);
       uint32_t run = 0, sum = 0;
-      for (uint32_t j = 0; j < per; ++j)
+      for (uint32_t j = 0; j < gper; ++j)
       {
-        if (first + j < nb)
+        if (first + j < groups)
         {
-          const uint32_t c = bins[first + j];
-          run              = c > run ? c : run;
-          sum += c;
+          const uint4 c = bins4[first + j];
+          run           = max(max(run, max(c.x, c.y)), max(c.z, c.w));
+          sum += c.x + c.y + c.z + c.w;
         }
       }
       uint32_t x = sum;
@@ -763,13 +770,21 @@ __device__ __forceinline__ void learned_bucket_body(const LearnedBucketParams& p
       {
         // bins[x] = start | count << 16
         uint32_t acc = base + x - sum;
-        for (uint32_t j = 0; j < per; ++j)
+        for (uint32_t j = 0; j < gper; ++j)
         {
-          if (first + j < nb)
+          if (first + j < groups)
           {
-            const uint32_t c = bins[first + j];
-            bins[first + j]  = acc | (c << 16);
-            acc += c;
+            const uint4 c = bins4[first + j];
+            uint4 o;
+            o.x = acc | (c.x << 16);
+            acc += c.x;
+            o.y = acc | (c.y << 16);
+            acc += c.y;
+            o.z = acc | (c.z << 16);
+            acc += c.z;
+            o.w = acc | (c.w << 16);
+            acc += c.w;
+            bins4[first + j] = o;
           }
         }
         __syncthreads();
