@@ -1076,6 +1076,7 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
     // ============================== look-back threads ==============================
     const int d                = tid - MT; // this thread's digit
     const uint32_t skip_tile   = gb300_fault_skip_tile; // no tile, unless a test withholds one
+    const unsigned long long bin_base = p.bins[d]; // the digit's global offset, the same for every tile
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
     {
       const uint32_t valid = min(uint32_t(TILE), p.portion_items - t * TILE);
@@ -1117,7 +1118,7 @@ __device__ __forceinline__ void onesweep_persistent_impl(const OnesweepParams& p
       {
         p.lookback_next[(size_t) (p.tile_row_base + t) * R + d] = 0u;
       }
-      const unsigned long long base = p.bins[d] + excl;
+      const unsigned long long base = bin_base + excl;
       gdelta[d]                     = (long long) base - (long long) start;
       if (p.bins_next != nullptr && t == p.portion_tiles - 1)
       {

@@ -1174,6 +1174,9 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
       const uint32_t row_base = g[SEG_GEO_BASE];
       const uint32_t si       = g[SEG_GEO_SEG];
       buf                     = buf == 2 ? 0 : buf + 1;
+      // the segment's digit offset, loaded now: its latency hides behind the tile's digit
+      // scan and look-back instead of delaying the offsets the main threads wait for
+      const unsigned long long seg_base = dp.seg_bins[((size_t) si * dp.num_passes + pass) * R + d];
       uint32_t start;
       const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start, d);
       if (uint32_t(d) == misc[4])
@@ -1242,7 +1245,7 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
       {
         lookback_next[(size_t) t * R + d] = 0u;
       }
-      const unsigned long long base = dp.seg_bins[((size_t) si * dp.num_passes + pass) * R + d] + excl;
+      const unsigned long long base = seg_base + excl;
       gdelta[d]                     = (long long) base - (long long) start;
       asm volatile("bar.arrive 5, %0;" ::"n"(TPB) : "memory"); // BG
     }
