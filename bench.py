@@ -778,6 +778,11 @@ def run_engine(args):
             torch.cuda.empty_cache()
         del flush_buf
 
+    floor = None
+    if not args.no_variants:
+        keys_only = next((v["onesweep_ms"] for v in variants if v["name"] == "u32 keys-only 2^28"), None)
+        floor = pattern_floor(peak, {"u64 keys + u32 values": onesweep_ms, "u32 keys only": keys_only})
+
     if rank != 0:
         return
     # CPU baseline: the reference's thrust OpenMP sort on a bounded sample (rank 0, N=1)
@@ -821,6 +826,7 @@ def run_engine(args):
                                 "mode": "one batch at a time: upload, sort, download"}},
         "cpu_baseline": cpu,
         "verified": verified,
+        "pattern_floor": floor,
         "variants": variants,
         "segmented": segmented,
         "learned": learned,
@@ -832,6 +838,74 @@ def main_bytes(n):
     return 8 * n * 2 * 12
 
 
+def _floor_lib():
+    import ctypes
+
+    from cccl_gb300.build import floor_library_path
+
+    lib = ctypes.CDLL(str(floor_library_path()))
+    lib.cccl_gb300_pattern_floor.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    lib.cccl_gb300_pattern_floor.restype = ctypes.c_int
+    return lib
+
+
+def _floor_run(lib, kb, vb, runs, shift=0, reps=5):
+    import ctypes
+
+    out = (ctypes.c_float * 3)()
+    rc = lib.cccl_gb300_pattern_floor(kb, vb, 1 << N_LOG2, runs, shift, reps, out)
+    if rc != 0:
+        raise RuntimeError(f"pattern floor: CUDA error {rc}")
+    return out[0], int(out[1]), int(out[2])
+
+
+def pattern_floor(peak, pass_ms, reps=5):
+    """The digit pass's memory-pattern floor for the tile shapes of the measured passes
+    (cccl_gb300/csrc/pattern_floor.cu): the pass's launch shape, tile and write-out without
+    the ranking and the look-back; one run per tile writes each staged tile back contiguously,
+    256 runs write its digit runs to their regions, as a pass over uniform keys does."""
+    lib = _floor_lib()
+    rows = []
+    for name, kb, vb in (("u64 keys + u32 values", 8, 4), ("u32 keys only", 4, 0)):
+        c_ms, tile, moved = _floor_run(lib, kb, vb, 1, reps=reps)
+        r_ms, _, _ = _floor_run(lib, kb, vb, 256, reps=reps)
+        nbytes = moved * 2 * (kb + vb)
+        pm = pass_ms.get(name)
+        rows.append({
+            "shape": name,
+            "keys_per_tile": tile,
+            "keys_per_digit_run": tile / 256,
+            "contiguous_ms": c_ms,
+            "contiguous_frac": nbytes / (c_ms / 1000.0) / 1e9 / peak,
+            "digit_runs_ms": r_ms,
+            "digit_runs_frac": nbytes / (r_ms / 1000.0) / 1e9 / peak,
+            "pass_ms": pm,
+            "pass_frac": nbytes / (pm / 1000.0) / 1e9 / peak if pm else None,
+            "pass_note": "headline pass" if kb == 8 else "mean of the sort's 4 passes (first one order-free)",
+        })
+    return {"num_items": 1 << N_LOG2, "unit_ms": "best of 5 launches, CUDA events", "rows": rows}
+
+
+def pattern_sweep():
+    """Run length and alignment of the write pattern at the keys-only tile (10752 u32 keys):
+    runs per tile, and runs of 32 keys (128 bytes) shifted by 0, 2 and 16 keys."""
+    peak, peak_kind = _peaks()
+    lib = _floor_lib()
+    rows = []
+    for runs, shift in ((1, 0), (64, 0), (128, 0), (224, 0), (256, 0), (336, 0), (336, 2), (336, 16), (512, 0)):
+        ms, tile, moved = _floor_run(lib, 4, 0, runs, shift)
+        rows.append({"runs_per_tile": runs, "keys_per_run": tile / runs, "shift_bytes": 4 * shift, "ms": ms,
+                     "frac": moved * 8 / (ms / 1000.0) / 1e9 / peak})
+    pairs = []
+    for runs in (1, 256):
+        ms, tile, moved = _floor_run(lib, 8, 4, runs)
+        pairs.append({"runs_per_tile": runs, "keys_per_run": tile / runs, "ms": ms,
+                      "frac": moved * 24 / (ms / 1000.0) / 1e9 / peak})
+    print(json.dumps({"pattern_sweep": rows, "keys_per_tile": 10752, "u64_u32_pairs_5760_tile": pairs,
+                      "num_items": 1 << N_LOG2, "peak_gbs": peak, "peak_source": peak_kind}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -840,11 +914,16 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile-case", choices=["pairs", "keys", "learned-f32", "learned-f64", "segmented"],
+    ap.add_argument("--profile-case", choices=["pairs", "keys", "learned-f32", "learned-f64", "segmented", "pattern-sweep"],
                     help="run untimed sorts for ncu captures: 2^--log2n u64+u32 pairs or u32 keys (two sorts), "
-                         "one learned sort of 2^--log2n lognormal f32+i32 / f64+i64 pairs, or the segmented workload")
+                         "one learned sort of 2^--log2n lognormal f32+i32 / f64+i64 pairs, or the segmented workload; "
+                         "pattern-sweep times the digit pass's write pattern by run length and alignment")
     ap.add_argument("--log2n", type=int, default=24)
     args = ap.parse_args()
+    if args.profile_case == "pattern-sweep":
+        ensure_built()
+        pattern_sweep()
+        return
     if args.profile_case:
         import torch
 

@@ -55,6 +55,10 @@ HOST_SOURCES = [
 ]
 # Runtime-API translation units (host + device code in one object, linked with static cudart)
 RUNTIME_SOURCES = ["noalloc_sort.cu"]
+# Measurement library of bench.py (the digit pass's memory-pattern floor), kept out of the
+# sort library
+FLOOR_SOURCE = "pattern_floor.cu"
+FLOOR_LIB_NAME = "libpatternfloor.so"
 
 
 def _digest(paths) -> str:
@@ -78,6 +82,10 @@ def library_path() -> Path:
     return BUILD / LIB_NAME
 
 
+def floor_library_path() -> Path:
+    return BUILD / FLOOR_LIB_NAME
+
+
 def build(verbose: bool = False, force: bool = False) -> Path:
     """Compile every kernel image for sm_103a and link the host library."""
     BUILD.mkdir(exist_ok=True)
@@ -87,7 +95,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     stamp = BUILD / "stamp.txt"
     digest = _digest(sources) + " ".join(TUNE_DEFINES)
     lib = library_path()
-    if not force and lib.exists() and stamp.exists() and stamp.read_text() == digest:
+    if not force and lib.exists() and floor_library_path().exists() and stamp.exists() and stamp.read_text() == digest:
         return lib
 
     def cubin(name_src):
@@ -139,9 +147,17 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         )
         return out
 
+    def floor_lib():
+        out = floor_library_path()
+        _run([NVCC, "-shared", *ARCH, *NVCC_FLAGS, *TUNE_DEFINES, "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-fvisibility=hidden", "-I", str(CSRC), str(CSRC / FLOOR_SOURCE), "-o", str(out) + ".tmp"], verbose)
+        shutil.move(str(out) + ".tmp", str(out))
+
     host = [CSRC / s for s in HOST_SOURCES] + [embed]
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        floor_job = ex.submit(floor_lib)
         objs = list(ex.map(host_obj, host)) + list(ex.map(runtime_obj, RUNTIME_SOURCES))
+        floor_job.result()
 
     libdirs = []
     for d in (CUDA_HOME / "lib64", CUDA_HOME / "lib64" / "stubs", CUDA_HOME / "targets" / "sbsa-linux" / "lib" / "stubs"):
