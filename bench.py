@@ -253,23 +253,31 @@ def kernel_times(torch, sorter, steps):
     return {r: statistics.mean(v) for r, v in out.items()}, launches_per_step
 
 
-def segmented_workload(seed=77, total=1 << 27):
+SEGMENTS_200K = 200_000
+
+
+def segmented_workload(seed=77, total=1 << 27, segments=None):
     """The batched segmented-sort configuration: f32 N(0,1) keys, 0.1% set to +-0.0/NaN, i32 values,
-    lognormal(5, 2.5) segment lengths clipped to [1, 2^23], 5% empty, int32 offsets."""
+    lognormal(5, 2.5) segment lengths clipped to [1, 2^23], 5% empty, int32 offsets. Lengths are
+    drawn until they add up to 2^27 keys (41,398 segments), or, with `segments`, that many
+    lengths are drawn and scaled to add up to 2^27 (the configuration's ~200k segments)."""
     import numpy as np
 
     import inputs as I
-    from segments import lognormal_segments
+    from segments import lognormal_segments, lognormal_segments_count
 
     rng = np.random.default_rng(seed)
-    b, e = lognormal_segments(rng, total)
+    if segments is None:
+        b, e = lognormal_segments(rng, total)
+    else:
+        b, e = lognormal_segments_count(rng, segments, total)
     n = int(e[-1])
     k = I.with_specials(rng.standard_normal(n).astype(np.float32), rng, 1e-3)
     v = rng.integers(-(2**31), 2**31 - 1, size=n, dtype=np.int32)
     return k, v, b.astype(np.int32), e.astype(np.int32)
 
 
-def run_segmented(torch, steps, per_segment_sample=None):
+def run_segmented(torch, steps, per_segment_sample=None, segments=None):
     """Batched segmented sort vs one plain radix-sort launch per segment (same GPU). The
     per-segment bar sorts every non-empty segment of the batch with its own plain sort call
     (per_segment_sample limits it to a sample, for profiling runs only)."""
@@ -277,7 +285,7 @@ def run_segmented(torch, steps, per_segment_sample=None):
 
     from cccl_gb300 import SortOrder, make_radix_sort, make_segmented_sort
 
-    k, v, b, e = segmented_workload()
+    k, v, b, e = segmented_workload(segments=segments)
     n, nseg = k.size, b.size
     kd = torch.from_numpy(k).cuda()
     vd = torch.from_numpy(v).cuda()
@@ -331,7 +339,8 @@ def run_segmented(torch, steps, per_segment_sample=None):
     peak, _ = _peaks()
     alg_bytes = 4 * n * 2 * 8
     return {
-        "workload": f"segmented SortPairs: 2^27 f32 keys (0.1% +-0/NaN) + i32 values, {nseg} lognormal(5,2.5) segments",
+        "workload": f"segmented SortPairs: 2^27 f32 keys (0.1% +-0/NaN) + i32 values, {nseg} lognormal(5,2.5) segments"
+                    + (" scaled to 2^27 keys" if segments is not None else ""),
         "num_items": n,
         "num_segments": int(nseg),
         "ms": ms,
@@ -726,6 +735,7 @@ def run_engine(args):
     learned = None
     if not args.no_variants:
         segmented = run_segmented(torch, max(3, args.steps // 2))
+        segmented["variant_200k_segments"] = run_segmented(torch, max(3, args.steps // 2), segments=SEGMENTS_200K)
         torch.cuda.empty_cache()
         learned = run_learned(torch, max(3, args.steps // 2))
 

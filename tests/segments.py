@@ -23,6 +23,21 @@ def lognormal_segments(rng, total, mu=5.0, sigma=2.5, lo=1, hi=1 << 23, empty_fr
     return ends - sizes, ends
 
 
+def lognormal_segments_count(rng, count, total, mu=5.0, sigma=2.5, lo=1, hi=1 << 23, empty_frac=0.05):
+    """`count` lengths lognormal(mu, sigma) clipped to [lo, hi], a fraction set to 0, then scaled
+    so that they add up to `total`: every non-empty length scaled and rounded down, at least
+    1, and the largest segment takes the difference. The segment count of a batch is kept and
+    its keys fit `total`."""
+    sizes = np.clip(rng.lognormal(mu, sigma, size=count), lo, hi)
+    sizes[rng.random(count) < empty_frac] = 0
+    scaled = np.floor(sizes * (total / sizes.sum())).astype(np.int64)
+    scaled[(sizes > 0) & (scaled < 1)] = 1
+    scaled[int(np.argmax(scaled))] += total - int(scaled.sum())
+    ends = np.cumsum(scaled)
+    assert ends[-1] == total
+    return ends - scaled, ends
+
+
 def edge_segments(sizes, gap=0):
     """Consecutive segments of the given sizes, optionally separated by uncovered gaps."""
     b, e, pos = [], [], 0

@@ -5,7 +5,8 @@ cases.
   entropy levels of the AND rule (1, 3 and 5 words), a constant key, descending, and the
   bit window 8..40 in both orders (the 2^28 headline itself is checked by bench.py on every
   run, with the GPU-side checker below).
-* The full batched segmented configuration (2^27 f32 + i32 pairs in lognormal segments)
+* The full batched segmented configuration (2^27 f32 + i32 pairs in lognormal segments:
+  41,398 segments drawn until they hold 2^27 keys, and 200,000 segments scaled to 2^27 keys)
   against the segmented oracle.
 * cub/test/catch2_test_device_radix_sort_keys.cu:488-519: num_items = 2^32 - 5 and 2^32 - 1
   (the 32-bit offset limit) and one size in (2^32, 2^33], u8 keys, both orders, checked as a
@@ -56,12 +57,14 @@ def test_sortpairs_u64_u32_at_2p24_vs_oracle(oracle, name, ands, constant, b, e,
     assert vo.tobytes() == rv.tobytes()
 
 
-def test_full_batched_segmented_configuration_vs_oracle(oracle):
+@pytest.mark.parametrize("segments", [None, 200_000], ids=["41398_segments", "200k_segments"])
+def test_full_batched_segmented_configuration_vs_oracle(oracle, segments):
     from bench import segmented_workload
     from gpu_util import gpu_seg_sort
 
-    k, v, b, e = segmented_workload()
+    k, v, b, e = segmented_workload(segments=segments)
     assert k.size == 1 << 27
+    assert b.size == (41398 if segments is None else segments)
     ko, vo, _ = gpu_seg_sort(k, v, b, e)
     rk, rv = oracle.segmented_sort(k, v, b, e, threads=16)
     assert ko.tobytes() == rk.tobytes()
