@@ -9,6 +9,7 @@ from .build import build, library_path
 from .radix_sort import DoubleBuffer, SortOrder, make_radix_sort, radix_sort, sort_status
 from .segmented_sort import make_segmented_radix_sort, make_segmented_sort, segmented_radix_sort, segmented_sort
 from .learned_sort import learned_sort, make_learned_sort
+from .distributed_sort import distributed_sort
 
 __all__ = [
     "build",
@@ -24,4 +25,5 @@ __all__ = [
     "segmented_radix_sort",
     "make_learned_sort",
     "learned_sort",
+    "distributed_sort",
 ]
