@@ -249,13 +249,17 @@ __device__ __forceinline__ void histogram_body(const HistogramParams& p)
 // Here the counter of (pass q, digit d) for lane l is its own word, laid out so that the 32
 // lanes of a warp always hit 32 different banks:
 //   byte offset = block(q) << 16 | d << 8 | byte0(q, l)
-//   q < 4:  block = q >> 1, byte0 = (q & 1) * 128 + l * 4        (32 columns)
-//   q >= 4: block = 2,      byte0 = (q & 3) * 64 + (l & 15) * 4  (16 columns, lanes l, l+16 share)
+//   up to 4 passes: block = q >> 1, byte0 = (q & 1) * 128 + l * 4 (32-bit counters)
+//   5 to 8 passes:  two passes share 32-bit words, pass 2p in the low and pass 2p + 1 in the
+//                   high 16 bits: block = q >> 2, byte0 = ((q >> 1) & 1) * 128 + l * 4
 // so one byte permute (digit byte q of the key into byte 1 of a per-lane constant) gives the
-// counter's address, and one reduction-add (no return value) counts the key: two
-// instructions per key and pass. Every CTA of the kernel shares the columns among its warps
-// (the adds are atomic). At the end each row of columns is summed by a warp and the totals go
-// to histogram_finish. Keys are streamed with four 16-byte loads in flight per thread.
+// counter's address, and one reduction-add (no return value; 1, or 1 << 16 for the high half)
+// counts the key: two instructions per key and pass, all 32 columns conflict-free for every
+// pass count. Every CTA of the kernel shares the columns among its warps (the adds are
+// atomic). The 16-bit halves are folded into 32-bit totals before they can overflow (every
+// warp adds at most one key per lane and counter per key it loads). At the end each row of
+// columns is summed by a warp and the totals go to histogram_finish. Keys are streamed with
+// four 16-byte loads in flight per thread.
 // ---------------------------------------------------------------------------------------
 // Encoded key for the counting loops: integer kinds have one mask for both signs (make_codec),
 // so their encoding is a single XOR; floating-point kinds pick the mask by the sign bit.
@@ -277,8 +281,9 @@ __device__ __forceinline__ U encode_key_for_count(U x, const KeyCodec& c)
 template <class U, int NP>
 __device__ __forceinline__ void count_digits_lanes(U t, uint32_t table_base, const uint32_t (&col)[8])
 {
-  const uint32_t lo = uint32_t(t);
-  uint32_t hi       = 0;
+  constexpr bool PACKED = NP > 4;
+  const uint32_t lo     = uint32_t(t);
+  uint32_t hi           = 0;
   if constexpr (sizeof(U) == 8)
   {
     hi = uint32_t((unsigned long long) t >> 32);
@@ -287,12 +292,62 @@ __device__ __forceinline__ void count_digits_lanes(U t, uint32_t table_base, con
   for (int q = 0; q < NP; ++q)
   {
     const uint32_t off = __byte_perm(q < 4 ? lo : hi, col[q], 0x7604u | (uint32_t(q & 3) << 4));
-    asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(table_base + off));
+    if (PACKED && (q & 1))
+    {
+      asm volatile("red.shared.add.u32 [%0], 65536;" ::"r"(table_base + off));
+    }
+    else
+    {
+      asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(table_base + off));
+    }
+  }
+}
+
+// Column counters of (pass, digit) in the layout above, summed over the 32 columns by one warp
+// per row, added to totals[pass * 256 + digit] and cleared. Called by the whole CTA.
+template <int TPB, int NP>
+__device__ __forceinline__ void histogram_lanes_fold(unsigned char* table, uint32_t* totals)
+{
+  constexpr int R      = RADIX_DIGITS;
+  constexpr bool PACKED = NP > 4;
+  constexpr int ROWS   = PACKED ? (NP + 1) / 2 : NP; // word rows: pass pairs, or passes
+  const int warp       = threadIdx.x >> 5;
+  const int lane       = threadIdx.x & 31;
+  for (int r = warp; r < ROWS * R; r += TPB / 32)
+  {
+    const int q          = r >> 8; // pass (pair, when packed)
+    const int d          = r & (R - 1);
+    const uint32_t base  = (uint32_t(q >> 1) << 16) | (uint32_t(d) << 8) | (uint32_t(q & 1) * 128u);
+    uint32_t* word       = reinterpret_cast<uint32_t*>(table + base + 4u * uint32_t(lane));
+    const uint32_t x     = *word;
+    *word                = 0u;
+    if constexpr (PACKED)
+    {
+      const uint32_t lo = __reduce_add_sync(0xffffffffu, x & 0xffffu);
+      const uint32_t hi = __reduce_add_sync(0xffffffffu, x >> 16);
+      if (lane == 0)
+      {
+        totals[(2 * q) * R + d] += lo;
+        if (2 * q + 1 < NP)
+        {
+          totals[(2 * q + 1) * R + d] += hi;
+        }
+      }
+    }
+    else
+    {
+      const uint32_t total = __reduce_add_sync(0xffffffffu, x);
+      if (lane == 0)
+      {
+        totals[q * R + d] += total;
+      }
+    }
   }
 }
 
 template <int KB, int FP, int TPB, int NP, bool WINDOW>
-__device__ __forceinline__ void histogram_lanes_count(const HistogramParams& p, uint32_t table_base, const uint32_t (&col)[8])
+__device__ __forceinline__ void
+histogram_lanes_count(const HistogramParams& p, unsigned char* table, uint32_t table_base, const uint32_t (&col)[8], uint32_t* totals)
 {
   using U           = typename uint_of<KB>::type;
   constexpr int VEC = 16 / KB; // keys per 16-byte load
@@ -341,24 +396,66 @@ __device__ __forceinline__ void histogram_lanes_count(const HistogramParams& p, 
       count_key(k[j]);
     }
   };
-  for (; v + 3 * stride < nvec; v += 4 * stride)
+  if constexpr (NP <= 4)
   {
-    uint4 w[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (; v + 3 * stride < nvec; v += 4 * stride)
     {
-      w[j] = __ldcs(vkeys + v + j * stride);
+      uint4 w[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        w[j] = __ldcs(vkeys + v + j * stride);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        count_vec(w[j]);
+      }
     }
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
+  }
+  else
+  {
+    // 16-bit counters: the CTA runs its first thread's trip count (the largest of its
+    // threads; the others skip what they have not got) and folds the counters every FOLD
+    // trips, before any half can pass 65535: a trip adds at most 4 * VEC keys per thread, so
+    // 32 warps x 4 * VEC x FOLD, plus the head, tail and remainder keys of a thread (at most
+    // 2 + 3 * VEC), stay below 2^16.
+    constexpr unsigned FOLD = 32768u / (32u * 4u * VEC) - 1u;
+    static_assert(32u * (4u * VEC * FOLD + 2u + 3u * VEC) < 65536u, "16-bit counters fold in time");
+    const unsigned long long v0 = blockIdx.x * (unsigned long long) TPB;
+    const unsigned long long trips =
+      v0 + 3 * stride < nvec ? (nvec - 3 * stride - v0 + 4 * stride - 1) / (4 * stride) : 0ull;
+    for (unsigned long long it = 0; it < trips; ++it)
     {
-      count_vec(w[j]);
+      if (v + 3 * stride < nvec)
+      {
+        uint4 w[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          w[j] = __ldcs(vkeys + v + j * stride);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          count_vec(w[j]);
+        }
+        v += 4 * stride;
+      }
+      if ((it + 1) % FOLD == 0u)
+      {
+        __syncthreads();
+        histogram_lanes_fold<TPB, NP>(table, totals);
+        __syncthreads();
+      }
     }
   }
   for (; v < nvec; v += stride)
   {
     count_vec(__ldcs(vkeys + v));
   }
+  __syncthreads();
+  histogram_lanes_fold<TPB, NP>(table, totals);
 }
 
 template <int KB, int FP, int TPB>
@@ -379,51 +476,40 @@ __device__ __forceinline__ void histogram_lanes_body(const HistogramParams& p)
   {
     *reinterpret_cast<uint4*>(table + i) = make_uint4(0u, 0u, 0u, 0u);
   }
-  uint32_t col[8]; // byte 0 and byte 2 of every pass's counter offsets for this lane
+  for (int i = tid; i < MAX_PASSES * R; i += TPB)
+  {
+    sh[i] = 0u;
+  }
+  // byte 0 and byte 2 of every pass's counter offsets for this lane (layout above)
+  uint32_t col[8];
+  const bool packed = P > 4;
 #pragma unroll
   for (int q = 0; q < 8; ++q)
   {
-    col[q] = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(q & 1) * 128u + uint32_t(lane) * 4u))
-                   : ((2u << 16) | (uint32_t(q & 3) * 64u + uint32_t(lane & 15) * 4u));
+    col[q] = packed ? ((uint32_t(q >> 2) << 16) | (uint32_t((q >> 1) & 1) * 128u + uint32_t(lane) * 4u))
+                    : ((uint32_t(q >> 1) << 16) | (uint32_t(q & 1) * 128u + uint32_t(lane) * 4u));
   }
   const uint32_t table_base = smem_addr(table);
   __syncthreads();
 
-  // the pass count is a compile-time constant of the counting loop: a whole key, or a window
+  // the pass count is a compile-time constant of the counting loop: a whole key, or a window;
+  // the loop leaves the CTA's counts of (pass, digit) in sh
   if (p.begin_bit == 0 && p.end_bit == 8 * KB)
   {
-    histogram_lanes_count<KB, FP, TPB, KB, false>(p, table_base, col);
+    histogram_lanes_count<KB, FP, TPB, KB, false>(p, table, table_base, col, sh);
   }
   else
   {
     switch (P)
     {
-      case 1: histogram_lanes_count<KB, FP, TPB, 1, true>(p, table_base, col); break;
-      case 2: if constexpr (KB >= 2) { histogram_lanes_count<KB, FP, TPB, 2, true>(p, table_base, col); } break;
-      case 3: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 3, true>(p, table_base, col); } break;
-      case 4: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 4, true>(p, table_base, col); } break;
-      case 5: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 5, true>(p, table_base, col); } break;
-      case 6: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 6, true>(p, table_base, col); } break;
-      case 7: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 7, true>(p, table_base, col); } break;
-      default: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 8, true>(p, table_base, col); } break;
-    }
-  }
-  __syncthreads();
-
-  // one warp per row of columns: the CTA's count of (pass, digit)
-  const int warp = tid >> 5;
-  for (int r = warp; r < P * R; r += TPB / 32)
-  {
-    const int q          = r >> 8;
-    const int d          = r & (R - 1);
-    const int width      = q < 4 ? 32 : 16;
-    const uint32_t base  = q < 4 ? ((uint32_t(q >> 1) << 16) | (uint32_t(d) << 8) | (uint32_t(q & 1) * 128u))
-                                 : ((2u << 16) | (uint32_t(d) << 8) | (uint32_t(q & 3) * 64u));
-    const uint32_t x     = lane < width ? *reinterpret_cast<const uint32_t*>(table + base + 4u * uint32_t(lane)) : 0u;
-    const uint32_t total = __reduce_add_sync(0xffffffffu, x);
-    if (lane == 0)
-    {
-      sh[r] = total;
+      case 1: histogram_lanes_count<KB, FP, TPB, 1, true>(p, table, table_base, col, sh); break;
+      case 2: if constexpr (KB >= 2) { histogram_lanes_count<KB, FP, TPB, 2, true>(p, table, table_base, col, sh); } break;
+      case 3: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 3, true>(p, table, table_base, col, sh); } break;
+      case 4: if constexpr (KB >= 4) { histogram_lanes_count<KB, FP, TPB, 4, true>(p, table, table_base, col, sh); } break;
+      case 5: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 5, true>(p, table, table_base, col, sh); } break;
+      case 6: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 6, true>(p, table, table_base, col, sh); } break;
+      case 7: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 7, true>(p, table, table_base, col, sh); } break;
+      default: if constexpr (KB >= 8) { histogram_lanes_count<KB, FP, TPB, 8, true>(p, table, table_base, col, sh); } break;
     }
   }
   histogram_finish<TPB>(p, sh);

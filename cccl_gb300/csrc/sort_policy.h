@@ -63,13 +63,13 @@ constexpr int HISTOGRAM_TPB    = 512;
 constexpr int HISTOGRAM_MINB   = 4;
 
 // Lane-column histogram of the plain sort (histogram_lanes_body): one CTA of 1024 threads per
-// SM; every lane owns a column of 32-bit counters per (pass, digit), so the 32 increments of
-// one warp instruction hit 32 different banks. Passes 0-3 get 32 columns (32 KB each), passes
-// 4-7 share 16 columns (16 KB each, two lanes per column: a two-way conflict).
+// SM; every lane owns a column of counters per (pass, digit), so the 32 increments of one warp
+// instruction hit 32 different banks. Up to 4 passes: 32-bit counters (32 KB a pass); 5 to 8
+// passes: two passes share each 32-bit word as 16-bit halves (32 KB a pair of passes).
 constexpr int HISTOGRAM_LANES_TPB = 1024;
 GB300_HD constexpr size_t histogram_table_bytes(int passes)
 {
-  return passes <= 2 ? size_t(65536) : passes <= 4 ? size_t(131072) : size_t(196608);
+  return passes <= 2 ? size_t(65536) : size_t(131072);
 }
 
 GB300_HD constexpr int onesweep_items(int kb, int vb)
