@@ -198,6 +198,7 @@ EXPORTED_SYMBOLS = [
     "cccl_gb300_learned_sort_cleanup",
     "cccl_gb300_learned_sort_set_route",
     "cccl_gb300_segmented_radix_sort",
+    "cccl_gb300_merge_sorted_runs",
     "cccl_gb300_sort_status",
     "cccl_gb300_testing_set_wait_fault",
 ]
@@ -238,6 +239,8 @@ def _declare(lib):
         P(C.c_int),
         C.c_void_p,
     ]
+    lib.cccl_gb300_merge_sorted_runs.argtypes = [RadixSortBuildResult, C.c_void_p, P(C.c_size_t), Iterator, Iterator,
+                                                 Iterator, Iterator, P(C.c_uint64), C.c_int, C.c_void_p]
     lib.cccl_device_radix_sort_link_ltoir.argtypes = [R, C.c_void_p, C.c_void_p, C.c_size_t]
     lib.cccl_device_radix_sort_serialize.argtypes = [R, P(C.c_void_p), P(C.c_size_t)]
     lib.cccl_device_radix_sort_deserialize.argtypes = [R, C.c_void_p, C.c_size_t]

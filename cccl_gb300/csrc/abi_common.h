@@ -196,7 +196,9 @@ inline void launch(
   const char* role, CUkernel kernel, unsigned grid, unsigned block, size_t smem, CUstream stream, const Params& p)
 {
   CUfunction f = function_of(kernel);
-  if (smem > 48 * 1024)
+  // dynamic shared memory near the 48 KB default leaves no room for a kernel's static shared
+  // memory: opt in above 47 KB
+  if (smem > 47 * 1024)
   {
     check(cuFuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, int(smem)),
           "cuFuncSetAttribute(max dynamic shared memory)");

@@ -5,6 +5,7 @@
 
 #include "radix_kernels.cuh"
 #include "gather_kernels.cuh"
+#include "merge_kernels.cuh"
 #include "sort_policy.h"
 
 #define GB300_CAT_(a, b) a##b
@@ -79,7 +80,8 @@
   GB300_SINGLE_TILE(KB, 4, FP, SUF)    \
   GB300_SINGLE_TILE(KB, 8, FP, SUF)    \
   GB300_SINGLE_TILE(KB, 16, FP, SUF)   \
-  GB300_HISTOGRAM(KB, FP, SUF)
+  GB300_HISTOGRAM(KB, FP, SUF)         \
+  GB300_MERGE_ALL_VALUES(KB, FP, SUF)
 
 extern "C" __global__ void __launch_bounds__(256) gb300_init(const gb300::InitParams p)
 {

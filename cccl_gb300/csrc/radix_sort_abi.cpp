@@ -8,9 +8,13 @@
 // special cases (:1950-2003): empty input, begin_bit == end_bit, single tile.
 #include <cccl/c/radix_sort.h>
 #include <cccl/c/serialization.h>
+#include <cccl_gb300/merge_runs.h>
 
 #include <algorithm>
 #include <memory>
+#include <string>
+#include <utility>
+#include <vector>
 
 #include "abi_common.h"
 #include "radix_plan.h"
@@ -534,6 +538,163 @@ try
 catch (const std::exception& e)
 {
   return report("cccl_device_radix_sort_cleanup", e);
+}
+
+// Stable merge of sorted runs (include/cccl_gb300/merge_runs.h): rounds of pairwise merges,
+// ping-ponging between the output and one buffer of temporary storage so that the last
+// round writes the output.
+CCCL_C_API CUresult cccl_gb300_merge_sorted_runs(
+  cccl_device_radix_sort_build_result_t build,
+  void* d_temp_storage,
+  size_t* temp_storage_bytes,
+  cccl_iterator_t d_keys_in,
+  cccl_iterator_t d_keys_out,
+  cccl_iterator_t d_values_in,
+  cccl_iterator_t d_values_out,
+  const uint64_t* run_offsets,
+  int num_runs,
+  CUstream stream)
+try
+{
+  if (d_keys_in.type != CCCL_POINTER || d_keys_out.type != CCCL_POINTER || d_values_in.type != CCCL_POINTER
+      || d_values_out.type != CCCL_POINTER)
+  {
+    return CUDA_ERROR_UNKNOWN;
+  }
+  if (temp_storage_bytes == nullptr || run_offsets == nullptr || num_runs < 1 || run_offsets[0] != 0)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  for (int r = 0; r < num_runs; ++r)
+  {
+    if (run_offsets[r + 1] < run_offsets[r])
+    {
+      return CUDA_ERROR_INVALID_VALUE;
+    }
+  }
+  context_guard ctx;
+  const RadixPolicy& pol = policy_of(build);
+  if (build.library == nullptr)
+  {
+    return CUDA_ERROR_NOT_INITIALIZED;
+  }
+  const bool has_values = d_values_in.state != nullptr;
+  if (has_values && (pol.gather_value_bytes > 0 || d_values_out.state == nullptr))
+  {
+    return pol.gather_value_bytes > 0 ? CUDA_ERROR_NOT_SUPPORTED : CUDA_ERROR_INVALID_VALUE;
+  }
+  const int kb         = pol.key_bytes;
+  const int vb         = has_values ? pol.value_bytes : 0;
+  const uint64_t n     = run_offsets[num_runs];
+  const size_t kbytes  = align_up(size_t(n) * kb, 256);
+  const size_t vbytes  = align_up(size_t(n) * vb, 256);
+  const uint64_t max_tiles = (n + MERGE_TILE - 1) / MERGE_TILE + 1; // of any pair in any round
+  const size_t need    = std::max<size_t>(1, kbytes + vbytes + align_up(size_t(max_tiles + 1) * 8, 256));
+  if (d_temp_storage == nullptr)
+  {
+    *temp_storage_bytes = need;
+    return CUDA_SUCCESS;
+  }
+  if (*temp_storage_bytes < need)
+  {
+    return CUDA_ERROR_INVALID_VALUE;
+  }
+  if (n == 0)
+  {
+    return CUDA_SUCCESS;
+  }
+  auto* tmp       = static_cast<unsigned char*>(d_temp_storage);
+  auto* out_keys  = static_cast<unsigned char*>(d_keys_out.state);
+  auto* out_vals  = static_cast<unsigned char*>(d_values_out.state);
+  const auto* src_keys = static_cast<const unsigned char*>(d_keys_in.state);
+  const auto* src_vals = static_cast<const unsigned char*>(d_values_in.state);
+  int rounds = 0;
+  while ((1 << rounds) < num_runs)
+  {
+    ++rounds;
+  }
+  if (rounds == 0)
+  {
+    check(cuMemcpyAsync(CUdeviceptr(out_keys), CUdeviceptr(src_keys), size_t(n) * kb, stream), "cuMemcpyAsync(keys)");
+    if (has_values)
+    {
+      check(cuMemcpyAsync(CUdeviceptr(out_vals), CUdeviceptr(src_vals), size_t(n) * vb, stream), "cuMemcpyAsync(values)");
+    }
+    return CUDA_SUCCESS;
+  }
+  const std::string name = "gb300_merge_k" + std::to_string(kb) + "_v" + std::to_string(vb) + "_"
+                         + (pol.key_kind == KIND_FLOAT ? "f" : "i");
+  const std::string split_name = "gb300_merge_split_k" + std::to_string(kb) + "_" + (pol.key_kind == KIND_FLOAT ? "f" : "i");
+  CUkernel merge = nullptr;
+  CUkernel split = nullptr;
+  check(cuLibraryGetKernel(&merge, build.library, name.c_str()), "cuLibraryGetKernel(merge)");
+  check(cuLibraryGetKernel(&split, build.library, split_name.c_str()), "cuLibraryGetKernel(merge split)");
+  auto* splits = reinterpret_cast<unsigned long long*>(tmp + kbytes + vbytes);
+  const KeyCodec codec = make_codec(pol.key_kind, kb, build.order == CCCL_DESCENDING);
+  const size_t smem    = merge_smem_bytes(kb, vb);
+  std::vector<std::pair<uint64_t, uint64_t>> runs; // [begin, end)
+  for (int r = 0; r < num_runs; ++r)
+  {
+    runs.emplace_back(run_offsets[r], run_offsets[r + 1]);
+  }
+  // an odd round count starts in the output, an even one in the temporary buffer
+  bool to_out = (rounds & 1) != 0;
+  for (int round = 0; round < rounds; ++round)
+  {
+    unsigned char* dk = to_out ? out_keys : tmp;
+    unsigned char* dv = to_out ? out_vals : tmp + kbytes;
+    std::vector<std::pair<uint64_t, uint64_t>> next;
+    for (size_t j = 0; j < runs.size(); j += 2)
+    {
+      const uint64_t a = runs[j].first;
+      if (j + 1 == runs.size())
+      {
+        // the odd run out moves unchanged
+        const uint64_t len = runs[j].second - a;
+        if (len > 0)
+        {
+          check(cuMemcpyAsync(CUdeviceptr(dk + a * kb), CUdeviceptr(src_keys + a * kb), size_t(len) * kb, stream),
+                "cuMemcpyAsync(keys)");
+          if (has_values)
+          {
+            check(cuMemcpyAsync(CUdeviceptr(dv + a * vb), CUdeviceptr(src_vals + a * vb), size_t(len) * vb, stream),
+                  "cuMemcpyAsync(values)");
+          }
+        }
+        next.push_back(runs[j]);
+        continue;
+      }
+      const uint64_t b = runs[j + 1].first, e = runs[j + 1].second;
+      MergeParams mp{};
+      mp.a_keys     = src_keys + a * kb;
+      mp.b_keys     = src_keys + b * kb;
+      mp.a_values   = has_values ? src_vals + a * vb : nullptr;
+      mp.b_values   = has_values ? src_vals + b * vb : nullptr;
+      mp.out_keys   = dk + a * kb;
+      mp.out_values = has_values ? dv + a * vb : nullptr;
+      mp.na         = b - a;
+      mp.nb         = e - b;
+      mp.codec      = codec;
+      mp.splits     = splits;
+      const uint64_t tiles = (e - a + MERGE_TILE - 1) / MERGE_TILE;
+      if (tiles > 0)
+      {
+        // the pairs of a round run one after another on the stream, so they share the splits
+        launch("merge_split", split, unsigned((tiles + 1 + 255) / 256), 256u, 0, stream, mp);
+        launch("merge", merge, unsigned(tiles), unsigned(MERGE_TPB), smem, stream, mp);
+      }
+      next.emplace_back(a, e);
+    }
+    runs     = std::move(next);
+    src_keys = dk;
+    src_vals = dv;
+    to_out   = !to_out;
+  }
+  return CUDA_SUCCESS;
+}
+catch (const std::exception& e)
+{
+  return report("cccl_gb300_merge_sorted_runs", e);
 }
 
 } // extern "C"

@@ -271,6 +271,21 @@ struct SegDeviceParams
   KeyCodec codec;
 };
 
+// ---- stable merge of two sorted runs (merge_kernels.cuh) ----
+struct MergeParams
+{
+  const void* a_keys; // run A: earlier in the stable order of equal keys
+  const void* b_keys;
+  const void* a_values; // null for keys-only
+  const void* b_values;
+  void* out_keys; // na + nb items, A and B merged
+  void* out_values;
+  unsigned long long na;
+  unsigned long long nb;
+  KeyCodec codec;
+  unsigned long long* splits; // A items before every tile's first output: [tiles + 1]
+};
+
 // ---- learned-partition sort ----
 constexpr int LEARNED_SAMPLE_LOG2 = 16;  // keys in the model's sample
 constexpr int LEARNED_SAMPLE      = 1 << LEARNED_SAMPLE_LOG2;

@@ -53,6 +53,15 @@ GB300_HD constexpr int persistent_main(int kb, int vb)
 {
   return persistent_tpb(kb, vb) - LOOKBACK_THREADS;
 }
+// Stable merge of two sorted runs (merge_kernels.cuh): one CTA per output tile.
+constexpr int MERGE_TPB   = 256;
+constexpr int MERGE_ITEMS = 8;
+constexpr int MERGE_TILE  = MERGE_TPB * MERGE_ITEMS;
+// A and B slices (one tile together) and the merged tile, keys and values each
+GB300_HD constexpr size_t merge_smem_bytes(int kb, int vb)
+{
+  return 2 * size_t(MERGE_TILE) * (size_t(kb) + size_t(vb));
+}
 constexpr int SINGLE_TILE_TPB  = 512;
 constexpr int SINGLE_TILE_ITEMS = 10;
 constexpr int HISTOGRAM_TPB    = 512;

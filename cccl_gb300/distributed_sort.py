@@ -21,9 +21,9 @@ The steps, each GB300-side work on the rank's own GPU:
      exact counts in place of sampled candidates;
   3. exchange: one all-to-all of the locally sorted keys (and values), each rank sending
      every other rank the run that falls into its slice (hss/data_exchange.h);
-  4. merge: the runs a rank receives arrive in rank order, each sorted, so a stable radix
-     sort of their concatenation is the merge (the reference merges them k ways,
-     hss/merge_k_way.h).
+  4. merge: the runs a rank receives arrive in rank order, each sorted; ceil(log2(ranks))
+     rounds of stable two-way merges on the GPU put them in order, equal keys in rank order
+     (cccl_gb300_merge_sorted_runs; the reference merges them k ways, hss/merge_k_way.h).
 
 Transport: ``torch.distributed`` collectives. With the NCCL backend the CUDA tensors are
 exchanged directly; with gloo (no GPU collectives) they are staged through host memory.
@@ -79,6 +79,23 @@ for _name, _signed in (("uint16", torch.int16), ("uint32", torch.int32)):
     if hasattr(torch, _name):
         _UNSIGNED_NARROW.add(getattr(torch, _name))
         _SIGNED_OF[getattr(torch, _name)] = _signed
+
+
+def _device_merge(keys: torch.Tensor, values: Optional[torch.Tensor], run_counts: list, descending: bool):
+    """Step 4: the stable pairwise merge of the received runs (cccl_gb300_merge_sorted_runs)."""
+    from .radix_sort import make_radix_sort
+
+    ko = torch.empty_like(keys)
+    vo = torch.empty_like(values) if values is not None else None
+    offsets = [0]
+    for c in run_counts:
+        offsets.append(offsets[-1] + int(c))
+    args = dict(d_in_keys=keys, d_out_keys=ko, d_in_values=values, d_out_values=vo)
+    s = make_radix_sort(order=SortOrder.DESCENDING if descending else SortOrder.ASCENDING, **args)
+    nbytes = s.merge_runs(temp_storage=None, run_offsets=offsets, **args)
+    temp = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=keys.device)
+    s.merge_runs(temp_storage=temp, run_offsets=offsets, **args)
+    return ko, vo
 
 
 def _device_radix_sort(keys: torch.Tensor, values: Optional[torch.Tensor], descending: bool):
@@ -243,8 +260,12 @@ def distributed_sort(
     rk = tr.all_to_all(ks, send, recv)
     rv = tr.all_to_all(vs, send, recv) if values is not None else None
 
-    # 4. merge of the rank-ordered runs: a stable sort of their concatenation
-    fk, fv = sort(rk, rv, descending)
+    # 4. merge of the rank-ordered runs: pairwise stable merges on the GPU (with a host-side
+    # local sort, a stable sort of their concatenation, which gives the same order)
+    if local_sort is None:
+        fk, fv = _device_merge(rk, rv, recv, descending)
+    else:
+        fk, fv = sort(rk, rv, descending)
     keys.copy_(fk)
     if values is not None:
         values.copy_(fv)

@@ -198,6 +198,37 @@ class _RadixSort:
         return temp_bytes.value
 
 
+def _merge_runs(self, *, temp_storage, d_in_keys, d_out_keys, d_in_values, d_out_values, run_offsets, stream=None) -> int:
+    """Stable merge of the sorted runs [run_offsets[r], run_offsets[r + 1]) of the inputs into the
+    outputs (cccl_gb300_merge_sorted_runs), in this build's order: equal keys keep run order.
+    ``temp_storage=None`` returns the temp-storage size."""
+    for t, n in ((d_in_keys, "keys in"), (d_out_keys, "keys out"), (d_in_values, "values in"),
+                 (d_out_values, "values out")):
+        _check_device_array(t, n)
+    offs = (C.c_uint64 * len(run_offsets))(*[int(x) for x in run_offsets])
+    if temp_storage is None:
+        temp_ptr, temp_bytes = None, C.c_size_t(0)
+    else:
+        temp_ptr, temp_bytes = temp_storage.data_ptr(), C.c_size_t(temp_storage.numel() * temp_storage.element_size())
+    rc = self.lib.cccl_gb300_merge_sorted_runs(
+        self.build_result,
+        temp_ptr,
+        C.byref(temp_bytes),
+        _key_iterator(d_in_keys),
+        _key_iterator(d_out_keys),
+        _value_iterator(d_in_values),
+        _value_iterator(d_out_values),
+        offs,
+        len(run_offsets) - 1,
+        _stream_handle(stream),
+    )
+    check(rc, "cccl_gb300_merge_sorted_runs")
+    return temp_bytes.value
+
+
+_RadixSort.merge_runs = _merge_runs
+
+
 def make_radix_sort(*, d_in_keys, d_out_keys, d_in_values, d_out_values, order: SortOrder) -> _RadixSort:
     """Builds a reusable radix sort for the given arrays' dtypes and ``order``."""
     return _RadixSort(d_in_keys, d_out_keys, d_in_values, d_out_values, order)
