@@ -603,6 +603,15 @@ try
   {
     return CUDA_SUCCESS;
   }
+  auto overlap = [](const void* a, const void* b, size_t bytes) {
+    const auto x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+    return x < y + bytes && y < x + bytes;
+  };
+  if (overlap(d_keys_in.state, d_keys_out.state, size_t(n) * kb)
+      || (has_values && overlap(d_values_in.state, d_values_out.state, size_t(n) * vb)))
+  {
+    return CUDA_ERROR_INVALID_VALUE; // the rounds read the inputs while writing the output
+  }
   auto* tmp       = static_cast<unsigned char*>(d_temp_storage);
   auto* out_keys  = static_cast<unsigned char*>(d_keys_out.state);
   auto* out_vals  = static_cast<unsigned char*>(d_values_out.state);

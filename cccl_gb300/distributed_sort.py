@@ -82,8 +82,13 @@ for _name, _signed in (("uint16", torch.int16), ("uint32", torch.int32)):
 
 
 def _device_merge(keys: torch.Tensor, values: Optional[torch.Tensor], run_counts: list, descending: bool):
-    """Step 4: the stable pairwise merge of the received runs (cccl_gb300_merge_sorted_runs)."""
+    """Step 4: the stable pairwise merge of the received runs (cccl_gb300_merge_sorted_runs).
+    Values of a width the merge kernels do not carry (not 1, 2, 4, 8 or 16 bytes) take the
+    radix sort of the concatenation instead, which gives the same order."""
     from .radix_sort import make_radix_sort
+
+    if values is not None and values.element_size() not in (1, 2, 4, 8, 16):
+        return _device_radix_sort(keys, values, descending)
 
     ko = torch.empty_like(keys)
     vo = torch.empty_like(values) if values is not None else None
