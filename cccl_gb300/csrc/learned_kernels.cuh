@@ -128,6 +128,70 @@ __device__ __forceinline__ uint32_t learned_bucket(U enc, const LearnedTables<U>
   return b < bmax ? b : bmax;
 }
 
+// learned_bucket for N keys at once, step by step across the keys: every phase (the cell
+// table, each step of the leaf search, the leaf line) issues its shared-memory reads for all
+// N keys before using any, so their latencies overlap instead of adding up key after key.
+// The search takes the same halving steps as learned_leaf (a cell's span is below 256, so at
+// most 8), and the bucket is the same value. Used by the model histogram, which streams the
+// keys (2^30 f64: 4.96 -> 4.34 ms on the lognormal/uniform mix, 3.91 -> 2.95 ms on sorted-then-
+// reversed keys); in the partition pass it made no difference (35.2 -> 35.8 ms), and the pass
+// keeps the key-by-key form, which needs fewer registers.
+template <class U, int FP, int N>
+__device__ __forceinline__ void
+learned_bucket_batch(const U (&enc)[N], uint32_t (&out)[N], const LearnedTables<U>& t, int range_log2, uint32_t bmax)
+{
+  U k[N];
+  int j[N];
+  int span[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+  {
+    k[i]             = digit_source<U, FP>(enc[i]);
+    const U d        = k[i] > t.kmin ? U(k[i] - t.kmin) : U(0);
+    const U c_wide   = d >> t.shift;
+    const uint32_t c = c_wide < U(LEARNED_CELLS - 1) ? uint32_t(c_wide) : uint32_t(LEARNED_CELLS - 1);
+    j[i]             = t.cell_leaf[c];
+    span[i]          = int(t.cell_leaf[c + 1]) - j[i];
+  }
+#pragma unroll
+  for (int step = 0; step < 8; ++step)
+  {
+    bool more = false;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+    {
+      if (span[i] > 0)
+      {
+        const int half = (span[i] + 1) >> 1;
+        if (t.leaf[j[i] + half].knot <= k[i])
+        {
+          j[i] += half;
+          span[i] -= half;
+        }
+        else
+        {
+          span[i] = half - 1;
+        }
+        more |= span[i] > 0;
+      }
+    }
+    if (!more)
+    {
+      break;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+  {
+    const LearnedLeaf<U> lf = t.leaf[j[i]];
+    const float x           = k[i] > lf.knot ? learned_to_float(U(k[i] - lf.knot)) : 0.0f;
+    const uint32_t lo       = uint32_t(j[i]) << range_log2;
+    uint32_t b              = __float2uint_rz(fmaf(lf.slope, x, lf.icpt));
+    b                       = min(max(b, lo), lo + (1u << range_log2));
+    out[i]                  = b < bmax ? b : bmax;
+  }
+}
+
 // log2 of the buckets in one leaf's rank range: (sample / leaves) * scale
 __host__ __device__ constexpr int learned_range_log2(int bucket_log2)
 {
@@ -338,8 +402,7 @@ __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
   const int range_log2 = learned_range_log2(p.bucket_log2);
   const uint32_t bmax  = (1u << p.bucket_log2) - 1u;
   const int passes     = p.h.num_passes;
-  auto count_key       = [&](U raw) {
-    const uint32_t b = learned_bucket<U, FP>(encode_key<U>(raw, p.h.codec), tables, range_log2, bmax);
+  auto count_bucket    = [&](uint32_t b) {
 #pragma unroll
     for (int q = 0; q < MAX_PASSES; ++q)
     {
@@ -349,7 +412,68 @@ __device__ __forceinline__ void learned_hist_body(const LearnedHistParams& p)
       }
     }
   };
-  histogram_for_each_key<KB, TPB>(p.h.keys, p.h.num_items, count_key);
+  auto count_key = [&](U raw) {
+    count_bucket(learned_bucket<U, FP>(encode_key<U>(raw, p.h.codec), tables, range_log2, bmax));
+  };
+  // the keys of several 16-byte loads (8 keys) are evaluated together (learned_bucket_batch),
+  // so the loads and the model's table reads of those keys are in flight at once
+  constexpr int VEC   = 16 / KB;
+  constexpr int LOADS = 8 / VEC;
+  const U* keys     = static_cast<const U*>(p.h.keys);
+  const unsigned long long n    = p.h.num_items;
+  const unsigned long long addr = reinterpret_cast<unsigned long long>(keys);
+  unsigned long long head       = ((16 - (addr & 15)) & 15) / KB;
+  head                          = head > n ? n : head;
+  const unsigned long long nvec     = (n - head) / VEC;
+  const unsigned long long body_end = head + nvec * VEC;
+  if (blockIdx.x == 0)
+  {
+    for (unsigned long long i = threadIdx.x; i < head; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+    for (unsigned long long i = body_end + threadIdx.x; i < n; i += TPB)
+    {
+      count_key(keys[i]);
+    }
+  }
+  const uint4* vkeys              = reinterpret_cast<const uint4*>(keys + head);
+  const unsigned long long stride = (unsigned long long) gridDim.x * TPB;
+  unsigned long long v            = blockIdx.x * (unsigned long long) TPB + threadIdx.x;
+  for (; v + (LOADS - 1) * stride < nvec; v += LOADS * stride)
+  {
+    uint4 w[LOADS];
+#pragma unroll
+    for (int g = 0; g < LOADS; ++g)
+    {
+      w[g] = __ldcs(vkeys + v + g * stride);
+    }
+    U k[LOADS * VEC];
+    memcpy(k, w, sizeof(w));
+#pragma unroll
+    for (int i = 0; i < LOADS * VEC; ++i)
+    {
+      k[i] = encode_key<U>(k[i], p.h.codec);
+    }
+    uint32_t b[LOADS * VEC];
+    learned_bucket_batch<U, FP, LOADS * VEC>(k, b, tables, range_log2, bmax);
+#pragma unroll
+    for (int i = 0; i < LOADS * VEC; ++i)
+    {
+      count_bucket(b[i]);
+    }
+  }
+  for (; v < nvec; v += stride)
+  {
+    const uint4 w = __ldcs(vkeys + v);
+    U k[VEC];
+    memcpy(k, &w, 16);
+#pragma unroll
+    for (int i = 0; i < VEC; ++i)
+    {
+      count_key(k[i]);
+    }
+  }
   histogram_finish<TPB>(p.h, sh);
 }
 
