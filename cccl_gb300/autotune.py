@@ -160,7 +160,7 @@ def measure(group):
 
 
 # ---------------------------------------------------------------------------------------
-# driver
+# the tuning loop: rebuild per candidate, measure, record
 # ---------------------------------------------------------------------------------------
 def _build(defines):
     env = dict(os.environ, GB300_TUNE_DEFINES=defines)
