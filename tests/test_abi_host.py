@@ -312,3 +312,30 @@ def test_segmented_offset_iterator_rejections(lib):
     unnamed.advance.name = b"bad name"
     unnamed._keep.append(unnamed.advance.name)
     assert compile_with(unnamed) == B.CUDA_ERROR_INVALID_VALUE
+
+
+def test_merge_sorted_runs_argument_checks(lib):
+    """cccl_gb300_merge_sorted_runs rejects, before touching the GPU: iterators that are not
+    pointers, a missing size pointer, and run offsets that are missing, empty, not starting
+    at 0 or decreasing."""
+    from cccl_gb300 import _bindings as B
+
+    rc, build = _compile(lib, (B.UINT64, 8), (B.UINT32, 4))
+    assert rc == B.CUDA_SUCCESS
+    keys = B.pointer_iterator(0x1000, B.UINT64, 8)
+    vals = B.pointer_iterator(0x2000, B.UINT32, 4)
+    temp = C.c_size_t(0)
+
+    def call(offsets, num_runs, k=keys, tb=C.byref(temp)):
+        arr = (C.c_uint64 * len(offsets))(*offsets) if offsets is not None else None
+        return lib.cccl_gb300_merge_sorted_runs(build, None, tb, k, k, vals, vals, arr, num_runs, None)
+
+    it = B.Iterator()
+    it.type = 1  # an iterator kind other than a pointer
+    assert call([0, 4, 8], 2, k=it) == B.CUDA_ERROR_UNKNOWN
+    assert call([0, 4, 8], 2, tb=None) == B.CUDA_ERROR_INVALID_VALUE
+    assert call(None, 2) == B.CUDA_ERROR_INVALID_VALUE
+    assert call([0], 0) == B.CUDA_ERROR_INVALID_VALUE
+    assert call([1, 4, 8], 2) == B.CUDA_ERROR_INVALID_VALUE
+    assert call([0, 8, 4], 2) == B.CUDA_ERROR_INVALID_VALUE
+    lib.cccl_device_radix_sort_cleanup(C.byref(build))

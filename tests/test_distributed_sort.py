@@ -8,7 +8,7 @@ values are global indices (the order of equal keys) and floats with +-0.0 and Na
 expected result is the oracle's radix sort of the rank-major concatenation of the inputs,
 each rank holding as many items as it passed.
 
-* CPU: two and three gloo ranks, the oracle as every rank's local sort (the distributed
+* CPU: two, three and four gloo ranks, the oracle as every rank's local sort (the distributed
   steps: splitter search, exchange, merge order).
 * GPU: two ranks in two processes on the one GPU, the library's radix sort as the local
   sort, the exchange through host memory (gloo); no kernel of one rank waits on the other.
@@ -125,7 +125,7 @@ def _rank_main(rank, world, port, device_sort):
         dist.destroy_process_group()
 
 
-@pytest.mark.parametrize("world", [2, 3])
+@pytest.mark.parametrize("world", [2, 3, 4])
 def test_distributed_sort_on_gloo_ranks(world, oracle):
     import torch.multiprocessing as mp
 
