@@ -509,7 +509,7 @@ LearnedStats learned_sort_stats(const LearnedSetup& s, const RadixCall& c)
   check(cuMemcpyDtoH(bucket_ctrs, CUdeviceptr(static_cast<unsigned char*>(c.d_temp_storage) + t.bounds_off),
                      sizeof(bucket_ctrs)),
         "cuMemcpyDtoH(learned stats)");
-  st.block_buckets = bucket_ctrs[1] + w[SEG_CTR_SMALL] + w[SEG_CTR_MEDIUM] + w[SEG_CTR_BLOCK_S] + w[SEG_CTR_BLOCK_L];
+  st.block_buckets = bucket_ctrs[1] + w[SEG_CTR_SMALL] + w[SEG_CTR_MEDIUM] + w[SEG_CTR_BLOCK_XS] + w[SEG_CTR_BLOCK_S] + w[SEG_CTR_BLOCK_L];
   st.device_buckets = w[SEG_CTR_DEVICE];
   std::memcpy(&st.device_items, &w[SEG_CTR_DEVICE_ITEMS], sizeof(st.device_items));
   return st;

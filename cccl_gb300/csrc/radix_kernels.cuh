@@ -568,8 +568,12 @@ __device__ __forceinline__ void block_sort_body(
   const U* kin     = static_cast<const U*>(keys_in);
 
   __syncthreads();
+  // warps whose keys are all padding keep them in place: they rank after every real key, and
+  // their slots are never read, so only the active warps' slots are filled
+  const int active_warps = int((n + ITEMS * 32 - 1) / (ITEMS * 32));
+  const int filled       = active_warps * ITEMS * 32;
   U kor = U(0), kand = U(~U(0)); // over the real keys' digit sources
-  for (int s = tid; s < TILE; s += TPB)
+  for (int s = tid; s < filled; s += TPB)
   {
     U k = U(~U(0));
     if (uint32_t(s) < n)
@@ -618,8 +622,6 @@ __device__ __forceinline__ void block_sort_body(
   __syncthreads(); // whist is zeroed by the first pass
   const int lo_bit = vary == 0 ? 0 : __ffsll((long long) vary) - 1;
   const int hi_bit = vary == 0 ? 0 : 64 - __clzll((long long) vary);
-  // warps whose keys are all padding keep them in place: they rank after every real key
-  const int active_warps = int((n + ITEMS * 32 - 1) / (ITEMS * 32));
 
   int cur = 0;
   for (int bit = lo_bit; bit < hi_bit; bit += BITS)

@@ -46,7 +46,14 @@ extern "C" __global__ void __launch_bounds__(256) gb300_seg_scan(const gb300::Se
                   || gb300::BlockMergeSmem<KB, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)>::bytes      \
                        == gb300::block_merge_smem(KB, gb300::seg_block_l_tpb(KB), gb300::seg_block_l_items(KB)),     \
                 "block merge shared-memory layout");                                                                 \
-  extern "C" __global__ void __launch_bounds__(gb300::seg_block_s_tpb(KB), gb300::seg_block_minb(KB))              \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_block_xs_tpb(KB), gb300::seg_block_xs_minb(KB))            \
+    gb300_seg_block_xs_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                            \
+  {                                                                                                                  \
+    gb300::seg_block_body<KB, VB, FP, gb300::seg_block_xs_tpb(KB), gb300::seg_block_xs_items(KB),                    \
+                          gb300::seg_block_s_bits(KB)>(                                                            \
+      p, p.block_xs_list, gb300::SEG_CTR_BLOCK_XS, gb300::SEG_CTR_TICKET_BLOCK_XS);                                  \
+  }                                                                                                                  \
+  extern "C" __global__ void __launch_bounds__(gb300::seg_block_s_tpb(KB), gb300::seg_block_s_minb(KB, VB))              \
     gb300_seg_block_s_k##KB##_v##VB##_##FS(const gb300::SegSortParams p)                                             \
   {                                                                                                                  \
     gb300::seg_block_body<KB, VB, FP, gb300::seg_block_s_tpb(KB), gb300::seg_block_s_items(KB),               \

@@ -65,7 +65,7 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
       b    = load_offset(p.begin_offsets, s, p.offsets_64);
       size = load_offset(p.end_offsets, s, p.offsets_64) - b;
     }
-    int cls = -1; // 0 small, 1 medium, 2 block small, 3 block large, 4 device
+    int cls = -1; // 0 small, 1 medium, 2 block small, 3 block large, 4 device, 5 block extra small
     if (size > 0 && (b < 0 || (unsigned long long) (b + size) > p.num_items))
     {
       atomicOr(p.status, STATUS_BAD_SEGMENT); // outside the keys: not sorted, never touched
@@ -76,6 +76,10 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
       if (size <= p.medium_tile)
       {
         cls = (p.partition && size <= p.small_tile) ? 0 : 1;
+      }
+      else if (size <= p.block_xs_cap)
+      {
+        cls = 5;
       }
       else if (size <= p.block_small_cap)
       {
@@ -97,6 +101,7 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
     }
     warp_append(cls == 0, p.counters + SEG_CTR_SMALL, p.small_list, uint32_t(s));
     warp_append(cls == 1, p.counters + SEG_CTR_MEDIUM, p.medium_list, uint32_t(s));
+    warp_append(cls == 5, p.counters + SEG_CTR_BLOCK_XS, p.block_xs_list, uint32_t(s));
     warp_append(cls == 2, p.counters + SEG_CTR_BLOCK_S, p.block_s_list, uint32_t(s));
     warp_append(cls == 3, p.counters + SEG_CTR_BLOCK_L, p.block_l_list, uint32_t(s));
     if (cls == 4)
@@ -608,6 +613,14 @@ __device__ __forceinline__ void seg_device_histogram_body(const SegDeviceParams&
   // with overlapping segments the lists may be incomplete: do no large-segment work at all
   const uint32_t ntiles = (*p.status & STATUS_SEG_CAPACITY) ? 0u : p.counters[SEG_CTR_DEVICE_TILES];
   const int tid         = threadIdx.x;
+  // the whole key in 8-bit digits from bit 0 (no bit window, no split pass): digit q is byte q
+  bool bytewise = p.num_passes == KB;
+  for (int q = 0; q < p.num_passes; ++q)
+  {
+    bytewise = bytewise && p.pass_bit[q] == 8 * q && p.pass_bits[q] == 8;
+  }
+  // keys in flight per thread in the byte-digit loop: 32 bytes
+  constexpr int LOADS = KB >= 8 ? 4 : 32 / KB > 8 ? 8 : 32 / KB;
 
   for (unsigned long long i = blockIdx.x * (unsigned long long) TPB + tid; i < (unsigned long long) ntiles * R;
        i += (unsigned long long) gridDim.x * TPB)
@@ -638,33 +651,77 @@ __device__ __forceinline__ void seg_device_histogram_body(const SegDeviceParams&
     const uint32_t valid     = min(p.device_tile, seg.size - first);
     const U* keys            = static_cast<const U*>(p.keys_in) + seg.begin + first;
     const uint32_t sh_base   = smem_addr(sh);
-    auto count_key           = [&](U raw) {
-      const U k = encode_key<U>(raw, p.codec);
-      for (int q = 0; q < p.num_passes; ++q)
-      {
-        const uint32_t d = extract_digit<U, FP>(k, p.pass_bit[q], (1u << p.pass_bits[q]) - 1u);
-        asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(sh_base + 4u * uint32_t(q * R + int(d))));
-      }
-    };
-    // four loads in flight per thread
-    uint32_t i = tid;
-    for (; i + 3u * TPB < valid; i += 4u * TPB)
+    if (bytewise)
     {
-      U k[4];
+      // digit q is byte q of the digit source: one byte permute and one address add per pass
+      auto count_key = [&](U raw) {
+        const U k         = digit_source<U, FP>(encode_key<U>(raw, p.codec));
+        const uint32_t lo = uint32_t(k);
+        uint32_t hi       = 0;
+        if constexpr (KB == 8)
+        {
+          hi = uint32_t((unsigned long long) k >> 32);
+        }
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
+        for (int q = 0; q < KB; ++q)
+        {
+          const uint32_t d = __byte_perm(q < 4 ? lo : hi, 0u, 0x4440u | uint32_t(q & 3));
+          asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(sh_base + uint32_t(q * R * 4) + 4u * d));
+        }
+      };
+      // LOADS loads in flight per thread, the tile's ragged end included (a tile is about two
+      // such batches per thread: one key at a time, its end would cost a load latency per key)
+      for (uint32_t i = tid; i < valid; i += LOADS * TPB)
       {
-        k[j] = __ldcs(keys + i + j * TPB);
-      }
+        U k[LOADS];
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-      {
-        count_key(k[j]);
+        for (int j = 0; j < LOADS; ++j)
+        {
+          if (i + j * TPB < valid)
+          {
+            k[j] = __ldcs(keys + i + j * TPB);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < LOADS; ++j)
+        {
+          if (i + j * TPB < valid)
+          {
+            count_key(k[j]);
+          }
+        }
       }
     }
-    for (; i < valid; i += TPB)
+    else
     {
-      count_key(keys[i]);
+      auto count_key = [&](U raw) {
+        const U k = encode_key<U>(raw, p.codec);
+        for (int q = 0; q < p.num_passes; ++q)
+        {
+          const uint32_t d = extract_digit<U, FP>(k, p.pass_bit[q], (1u << p.pass_bits[q]) - 1u);
+          asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(sh_base + 4u * uint32_t(q * R + int(d))));
+        }
+      };
+      // four loads in flight per thread
+      uint32_t i = tid;
+      for (; i + 3u * TPB < valid; i += 4u * TPB)
+      {
+        U k[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          k[j] = __ldcs(keys + i + j * TPB);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          count_key(k[j]);
+        }
+      }
+      for (; i < valid; i += TPB)
+      {
+        count_key(keys[i]);
+      }
     }
     __syncthreads();
     for (int i = tid; i < p.num_passes * R; i += TPB)
@@ -881,10 +938,9 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
   uint32_t* lookback      = dp.lookback[pass & 1];
   uint32_t* lookback_next = (pass + 1 < dp.num_passes) ? dp.lookback[(pass + 1) & 1] : nullptr;
 
-  // thread 0: the geometry of tile t into slot b, and its bulk copy when it can have one
-  auto issue = [&](uint32_t t, int b) {
-    const uint32_t si       = dp.tile_segment[t];
-    const DeviceSegment seg = dp.device_list[si];
+  // thread 0: the geometry of tile t (of segment si, seg) into slot b, and its bulk copy when
+  // it can have one
+  auto issue = [&](uint32_t t, uint32_t si, const DeviceSegment& seg, int b) {
     const uint32_t local    = t - seg.tile_base;
     const uint32_t first    = local * uint32_t(TILE);
     const uint32_t valid    = min(uint32_t(TILE), seg.size - first);
@@ -932,7 +988,8 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
     misc[2] = 0u;
     if (blockIdx.x < ntiles)
     {
-      issue(blockIdx.x, 0);
+      const uint32_t si = dp.tile_segment[blockIdx.x];
+      issue(blockIdx.x, si, dp.device_list[si], 0);
     }
   }
   for (int i = tid; i < NW * R; i += TPB)
@@ -1026,14 +1083,26 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
     int prev_buf        = 0;
     uint32_t prev_valid = 0;
     bool have_prev      = false;
+    // Thread 0 looks up the segment of the CTA's tile after next one iteration ahead, in two
+    // steps placed where warp 0 waits anyway (tile -> segment index after BH, segment record
+    // after BO): the two dependent loads then never delay the tile's histogram, and the
+    // barrier behind it, the way a lookup at the bulk copy's issue would.
+    uint32_t si_next = 0;
+    DeviceSegment seg_next{};
+    if (tid == 0 && blockIdx.x + gridDim.x < ntiles)
+    {
+      si_next  = dp.tile_segment[blockIdx.x + gridDim.x];
+      seg_next = dp.device_list[si_next];
+    }
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x)
     {
-      const uint32_t tn = t + gridDim.x;
-      const int nbuf    = buf == 2 ? 0 : buf + 1;
+      const uint32_t tn  = t + gridDim.x;
+      const uint32_t tnn = tn + gridDim.x; // < 2^32: tiles and grid are far below 2^31
+      const int nbuf     = buf == 2 ? 0 : buf + 1;
       if (tid == 0 && tn < ntiles)
       {
         fence_proxy_async_smem(); // buffer nbuf was last accessed by the generic proxy
-        issue(tn, nbuf);
+        issue(tn, si_next, seg_next, nbuf);
       }
 
       // ---- load (encode on the first pass; keys past the tile are all-ones: they rank last) ----
@@ -1096,12 +1165,23 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
           }
         }
       }
-      warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+      // a segment's last tile is partial: warps holding only padding do not count their keys
+      // (their rows stay zero; the look-back threads discount only the counted padding)
+      const bool live = uint32_t(warp) * uint32_t(ITEMS * 32) < valid;
+      if (live)
+      {
+        warp_histogram<U, FP, ITEMS>(keys, whist + warp * R, bit, dmask);
+      }
       if (tid == 0)
       {
         misc[4] = extract_digit<U, FP>(keys[0], bit, dmask);
       }
       asm volatile("bar.arrive 3, %0;" ::"n"(TPB) : "memory"); // BH: counts of t ready
+      uint32_t si_nn = 0;
+      if (tid == 0 && tnn < ntiles)
+      {
+        si_nn = dp.tile_segment[tnn];
+      }
 
       // ---- the previous tile goes out while the look-back threads turn t's counts into positions ----
       if (have_prev)
@@ -1110,8 +1190,14 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
         write_out(prev_buf, prev_valid);
       }
       asm volatile("bar.sync 4, %0;" ::"n"(TPB) : "memory"); // BO: positions of t in whist
+      if (tid == 0 && tnn < ntiles)
+      {
+        si_next  = si_nn;
+        seg_next = dp.device_list[si_nn];
+      }
 
       // ---- rank t, stage it in its own buffer (every main thread read it before BO) ----
+      // (padding-only warps rank their keys after every counted one, inside the tile)
       const uint32_t single = misc[3];
       uint32_t pos[ITEMS];
       if (single != 0u)
@@ -1181,9 +1267,11 @@ __device__ __forceinline__ void seg_device_persistent_body(const SegDeviceParams
       const uint32_t total = block_digit_offsets<NW>(whist, misc + 8, &start, d);
       if (uint32_t(d) == misc[4])
       {
-        // every real key of the tile has the first key's digit (padding keys, digit dmask,
-        // are discounted)
-        const uint32_t real = total - (uint32_t(d) == dmask ? uint32_t(TILE) - valid : 0u);
+        // every real key of the tile has the first key's digit (the counted padding keys, digit
+        // dmask, are discounted: the padding of the live warps, whole warps of 32 x ITEMS slots)
+        constexpr uint32_t WS  = uint32_t(ITEMS * 32);
+        const uint32_t counted = min(uint32_t(TILE), (valid + WS - 1) / WS * WS);
+        const uint32_t real    = total - (uint32_t(d) == dmask ? counted - valid : 0u);
         misc[3]             = real == valid ? (1u | (uint32_t(d) << 8)) : 0u;
       }
       uint32_t* col      = lookback + (size_t) row_base * R + d; // this segment's chain, digit d

@@ -47,7 +47,8 @@ void segmented_kernel_names(int kb, int vb, int kind, bool descending, char (&na
     "gb300_seg_pass_" + rad,
     "gb300_seg_small_" + kv + "r" + fs,
     "gb300_seg_medium_" + kv + "r" + fs,
-    "gb300_seg_ppass_" + rad};
+    "gb300_seg_ppass_" + rad,
+    "gb300_seg_block_xs_" + rad};
   for (int i = 0; i < SK_COUNT; ++i)
   {
     std::snprintf(names[i], sizeof(names[i]), "%s", n[i].c_str());
@@ -171,7 +172,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   off += align_up(4 * size_t(max_dev) * passes * RADIX_DIGITS, 256);
   const size_t zero_bytes  = off; // control block + per-segment counts are zeroed per call
   const size_t lists_off   = off;
-  off += 4 * align_up(4 * size_t(nseg), 256);
+  off += 5 * align_up(4 * size_t(nseg), 256); // one segment list per block or network class
   const size_t dev_off     = off;
   off += align_up(sizeof(DeviceSegment) * size_t(max_dev), 256);
   const size_t tseg_off    = off;
@@ -267,6 +268,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.max_tiles       = max_tiles;
     p.small_tile      = c.radix_only ? SEG_RSMALL_THREADS * SEG_RSMALL_ITEMS : pol.small_threads * pol.small_items;
     p.medium_tile     = c.radix_only ? SEG_RMEDIUM_THREADS * SEG_RMEDIUM_ITEMS : pol.medium_threads * pol.medium_items;
+    p.block_xs_cap    = SEG_BLOCK_XS_CAP;
     p.block_small_cap = pol.block_s_cap;
     p.block_large_cap = pol.block_l_cap;
     p.device_tile     = uint32_t(pass_tile);
@@ -275,6 +277,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.medium_list     = lists + list_stride;
     p.block_s_list    = lists + 2 * list_stride;
     p.block_l_list    = lists + 3 * list_stride;
+    p.block_xs_list   = lists + 4 * list_stride;
     p.device_list     = dev_list;
     p.tile_segment    = tseg;
     p.status          = status;
@@ -297,6 +300,7 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.medium_list   = lists + list_stride;
     p.block_s_list  = lists + 2 * list_stride;
     p.block_l_list  = lists + 3 * list_stride;
+    p.block_xs_list = lists + 4 * list_stride;
     p.codec         = codec;
     p.begin_bit     = begin_bit;
     p.end_bit       = end_bit;
@@ -312,6 +316,10 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     }
     launch("seg_medium", medium, unsigned(sms * occupancy(medium, SEG_NETWORK_TPB, medium_smem)), SEG_NETWORK_TPB,
            medium_smem, c.stream, p);
+    const int xs_tpb       = seg_block_xs_tpb(kb);
+    const uint64_t xs_smem = seg_block_smem(kb, xs_tpb, seg_block_xs_items(kb));
+    launch("seg_block_xs", ks.k[SK_BLOCK_XS], unsigned(sms * occupancy(ks.k[SK_BLOCK_XS], xs_tpb, xs_smem)),
+           unsigned(xs_tpb), xs_smem, c.stream, p);
     launch("seg_block_s", ks.k[SK_BLOCK_S], unsigned(sms * occupancy(ks.k[SK_BLOCK_S], pol.block_s_tpb, pol.block_s_smem)),
            unsigned(pol.block_s_tpb), pol.block_s_smem, c.stream, p);
     launch("seg_block_l", ks.k[SK_BLOCK_L], unsigned(sms * occupancy(ks.k[SK_BLOCK_L], pol.block_l_tpb, pol.block_l_smem)),

@@ -60,6 +60,7 @@ enum SegKernel : int
   SK_RSMALL,  // the networks in radix order (segmented radix sort, learned buckets)
   SK_RMEDIUM,
   SK_PPASS,   // the pipelined device-class pass
+  SK_BLOCK_XS, // block class of the shortest segments
   SK_COUNT
 };
 

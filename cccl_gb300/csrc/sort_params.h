@@ -188,6 +188,8 @@ enum : uint32_t
   SEG_CTR_TICKET_BLOCK_L,
   SEG_CTR_TICKET_HIST,
   SEG_CTR_TICKET_SCAN,
+  SEG_CTR_BLOCK_XS, // block class of the shortest segments (256 threads x 2 keys)
+  SEG_CTR_TICKET_BLOCK_XS,
   SEG_CTR_TICKET_PASS0, // one per device pass
   SEG_CTR_DEVICE_ITEMS = 30, // u64 (two words, 8-byte aligned): keys in device-class segments
   SEG_CTR_WORDS        = 32
@@ -213,6 +215,7 @@ struct SegClassifyParams
   unsigned long long max_tiles;           // capacity of tile_segment
   long long small_tile;
   long long medium_tile;
+  long long block_xs_cap;
   long long block_small_cap;
   long long block_large_cap;
   uint32_t device_tile;
@@ -220,6 +223,7 @@ struct SegClassifyParams
   uint32_t* counters;
   uint32_t* small_list;
   uint32_t* medium_list;
+  uint32_t* block_xs_list;
   uint32_t* block_s_list;
   uint32_t* block_l_list;
   DeviceSegment* device_list;
@@ -240,6 +244,7 @@ struct SegSortParams
   uint32_t* counters;
   const uint32_t* small_list;
   const uint32_t* medium_list;
+  const uint32_t* block_xs_list;
   const uint32_t* block_s_list;
   const uint32_t* block_l_list;
   KeyCodec codec;

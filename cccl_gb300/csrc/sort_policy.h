@@ -306,6 +306,18 @@ GB300_HD constexpr int seg_block_minb(int kb)
   return kb == 4 ? 2 : 1;
 #endif
 }
+// block_s (256 threads) sized for more CTAs per SM than block_l: its segments are short and
+// its CTAs spend most of their time in barriers, so resident CTAs hide each other's waits.
+// 4-byte keys with values of up to 4 bytes: 48 registers, five CTAs per SM (64 registers held
+// it at four; with 8-byte values 48 registers spill).
+GB300_HD constexpr int seg_block_s_minb(int kb, int vb)
+{
+#ifdef GB300_SEG_BLOCK_S_MINB
+  return (void) kb, (void) vb, GB300_SEG_BLOCK_S_MINB;
+#else
+  return kb == 4 && vb <= 4 ? 5 : seg_block_minb(kb);
+#endif
+}
 GB300_HD constexpr int seg_block_s_items(int kb)
 {
   return (void) kb, 8;
@@ -348,6 +360,27 @@ GB300_HD constexpr int seg_block_l_tpb(int kb)
 {
   return SEG_BLOCK_L_CAP / seg_block_l_items(kb);
 }
+// block_xs: segments longer than the medium network's tile and up to 512 keys, one CTA of
+// 256 threads x 2 keys each (one thread per digit, as every block pass needs). Small
+// registers and shared memory keep eight CTAs resident per SM (four-byte keys), against four
+// or five of block_s, whose 2048-key tile would be mostly padding for these segments.
+constexpr int SEG_BLOCK_XS_CAP = 512;
+GB300_HD constexpr int seg_block_xs_items(int kb)
+{
+  return (void) kb, 2;
+}
+GB300_HD constexpr int seg_block_xs_tpb(int kb)
+{
+  return SEG_BLOCK_XS_CAP / seg_block_xs_items(kb);
+}
+GB300_HD constexpr int seg_block_xs_minb(int kb)
+{
+#ifdef GB300_SEG_BLOCK_XS_MINB
+  return (void) kb, GB300_SEG_BLOCK_XS_MINB;
+#else
+  return kb == 8 ? 6 : 8;
+#endif
+}
 constexpr int SEG_NETWORK_TPB   = 256;
 // Device-class digit pass (CTA per tile): threads and items per thread; GB300_SEG_PASS_*
 // override them in tuning builds. Measured (cccl_gb300/autotune.py, cccl_gb300/tuning_gb300.json,
@@ -386,12 +419,12 @@ GB300_HD constexpr size_t seg_persistent_smem_for(int kb, int vb, int tpb, int i
 }
 GB300_HD constexpr int seg_ppass_items(int kb, int vb)
 {
-  // 4-byte keys: capped where the plain pass's item counts spilled registers here (the tile
-  // geometry and the offset reads take a few more)
+  // 4-byte keys: capped where the plain pass's item counts spill registers here (the tile
+  // geometry and the offset reads take a few more): 14 keys-only and 13 with values spill
 #ifdef GB300_SEG_PPASS_ITEMS
   int items = GB300_SEG_PPASS_ITEMS;
 #else
-  int items = kb == 4 ? (vb == 0 ? 12 : vb == 4 ? 11 : persistent_items_nominal(kb, vb)) : persistent_items_nominal(kb, vb);
+  int items = kb == 4 ? (vb == 0 ? 13 : vb == 4 ? 12 : persistent_items_nominal(kb, vb)) : persistent_items_nominal(kb, vb);
 #endif
   while (items > 1 && seg_persistent_smem_for(kb, vb, seg_ppass_tpb(kb, vb), items) > size_t(227) * 1024)
   {

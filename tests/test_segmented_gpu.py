@@ -36,7 +36,8 @@ def _nan_keys(dtype, n, rng, density=1 / 8):
     return I.with_specials(I.finite_floats(dtype, n, rng), rng, density)
 
 
-EDGE_SIZES = [1, 2, 3, 4, 17, 18, 19, 20, 111, 112, 113, 200, 2047, 2048, 2049, 8191, 8192, 8193, 20000, 100_000]
+EDGE_SIZES = [1, 2, 3, 4, 17, 18, 19, 20, 111, 112, 113, 200, 511, 512, 513, 2047, 2048, 2049, 8191, 8192, 8193, 20000,
+              100_000]
 
 
 @pytest.mark.parametrize("many", [False, True], ids=["fallback", "partitioned"])
@@ -142,7 +143,7 @@ def test_segmented_radix_sort(oracle, bits, desc, overwrite):
     from gpu_util import gpu_seg_sort
 
     rng = np.random.default_rng(31 + desc + 2 * overwrite)
-    b, e = edge_segments([1, 17, 112, 113, 2048, 2049, 8193, 30000, 5, 0, 700], gap=3)[:2]
+    b, e = edge_segments([1, 17, 112, 113, 256, 257, 512, 513, 2048, 2049, 8193, 30000, 5, 0, 700], gap=3)[:2]
     n = int(e[-1]) + 5
     k = I.with_specials(I.finite_floats(np.float32, n, rng), rng, 1 / 16)
     v = I.index_values(n)
