@@ -791,7 +791,14 @@ def run_engine(args):
     floor = None
     if not args.no_variants:
         keys_only = next((v["onesweep_ms"] for v in variants if v["name"] == "u32 keys-only 2^28"), None)
-        floor = pattern_floor(peak, {"u64 keys + u32 values": onesweep_ms, "u32 keys only": keys_only})
+        # the plain sort of the learned workloads' 2^28 f32 + u32 pairs: the mean of its passes
+        f32_pairs = None
+        if learned:
+            row = learned[0]
+            if row.get("plain_kernel_ms") and row.get("plain_passes_run"):
+                f32_pairs = row["plain_kernel_ms"]["onesweep"] / row["plain_passes_run"]
+        floor = pattern_floor(peak, {"u64 keys + u32 values": onesweep_ms, "u32 keys only": keys_only,
+                                     "f32 keys + u32 values": f32_pairs})
 
     if rank != 0:
         return
@@ -877,7 +884,7 @@ def pattern_floor(peak, pass_ms, reps=5):
     256 runs write its digit runs to their regions, as a pass over uniform keys does."""
     lib = _floor_lib()
     rows = []
-    for name, kb, vb in (("u64 keys + u32 values", 8, 4), ("u32 keys only", 4, 0)):
+    for name, kb, vb in (("u64 keys + u32 values", 8, 4), ("u32 keys only", 4, 0), ("f32 keys + u32 values", 4, 4)):
         c_ms, tile, moved = _floor_run(lib, kb, vb, 1, reps=reps)
         r_ms, _, _ = _floor_run(lib, kb, vb, 256, reps=reps)
         nbytes = moved * 2 * (kb + vb)
@@ -892,7 +899,8 @@ def pattern_floor(peak, pass_ms, reps=5):
             "digit_runs_frac": nbytes / (r_ms / 1000.0) / 1e9 / peak,
             "pass_ms": pm,
             "pass_frac": nbytes / (pm / 1000.0) / 1e9 / peak if pm else None,
-            "pass_note": "headline pass" if kb == 8 else "mean of the sort's 4 passes (first one order-free)",
+            "pass_note": "headline pass" if kb == 8 else "mean of the sort's 4 passes (first one order-free)"
+                         if vb == 0 else "mean of the 4 passes of the plain sort of the learned rows' 2^28 f32 + u32 (GMM)",
         })
     return {"num_items": 1 << N_LOG2, "unit_ms": "best of 5 launches, CUDA events", "rows": rows}
 
