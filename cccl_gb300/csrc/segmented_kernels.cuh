@@ -104,6 +104,7 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
     warp_append(cls == 5, p.counters + SEG_CTR_BLOCK_XS, p.block_xs_list, uint32_t(s));
     warp_append(cls == 2, p.counters + SEG_CTR_BLOCK_S, p.block_s_list, uint32_t(s));
     warp_append(cls == 3, p.counters + SEG_CTR_BLOCK_L, p.block_l_list, uint32_t(s));
+    uint32_t row = ~0u; // device-list index of this lane's segment, when it got one
     if (cls == 4)
     {
       const uint32_t tiles = uint32_t((size + p.device_tile - 1) / p.device_tile);
@@ -117,10 +118,26 @@ __device__ __forceinline__ void seg_classify_body(const SegClassifyParams& p)
         {
           p.tile_segment[base + t] = idx;
         }
+        row = idx;
       }
       else
       {
         atomicOr(p.status, STATUS_SEG_CAPACITY); // overlapping segments exceed the plan
+      }
+    }
+    // the warp clears the digit-count rows of its device segments (num_passes x 256 words
+    // each, 16-byte aligned), so the per-call clearing covers only segments that exist
+    uint32_t rows = __ballot_sync(0xffffffffu, row != ~0u);
+    const int words = p.num_passes * RADIX_DIGITS;
+    while (rows != 0u)
+    {
+      const int src   = __ffs(rows) - 1;
+      rows &= rows - 1u;
+      const uint32_t r = __shfl_sync(0xffffffffu, row, src);
+      uint4* w         = reinterpret_cast<uint4*>(p.seg_counts + (size_t) r * words);
+      for (int i = int(threadIdx.x & 31); i < words / 4; i += 32)
+      {
+        w[i] = make_uint4(0u, 0u, 0u, 0u);
       }
     }
   }

@@ -168,9 +168,9 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
   size_t off               = 0;
   const size_t ctrl_off    = off;
   off += align_up(4 * SEG_CTR_WORDS, 256);
+  const size_t zero_bytes  = off; // the control block is zeroed per call (classify clears the counts rows it uses)
   const size_t counts_off  = off;
   off += align_up(4 * size_t(max_dev) * passes * RADIX_DIGITS, 256);
-  const size_t zero_bytes  = off; // control block + per-segment counts are zeroed per call
   const size_t lists_off   = off;
   off += 5 * align_up(4 * size_t(nseg), 256); // one segment list per block or network class
   const size_t dev_off     = off;
@@ -281,6 +281,8 @@ void segmented_sort_dispatch(const SegmentedPolicy& pol, const SegmentedKernels&
     p.device_list     = dev_list;
     p.tile_segment    = tseg;
     p.status          = status;
+    p.seg_counts      = counts;
+    p.num_passes      = passes;
     launch("seg_classify", ks.k[SK_CLASSIFY], unsigned(std::min<uint64_t>(ceil_div(nseg, 256), uint64_t(sms) * 8)), 256,
            0, c.stream, p);
   }

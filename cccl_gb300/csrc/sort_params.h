@@ -229,6 +229,9 @@ struct SegClassifyParams
   DeviceSegment* device_list;
   uint32_t* tile_segment;
   uint32_t* status;
+  uint32_t* seg_counts; // [max_device_segments][num_passes][256]: a device segment's row is zeroed here
+  int num_passes;
+  int pad1;
 };
 
 struct SegSortParams
