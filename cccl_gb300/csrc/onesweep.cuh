@@ -83,7 +83,11 @@ struct PassIO
 
 // Resolves the pass's buffers. Returns false when the pass does nothing: gated off, or
 // skipped by its plan (its digit is the same for every key), in which case the grid first
-// clears this portion's rows of the next pass's look-back buffer, as the pass would have.
+// clears this portion's rows of the next pass's look-back buffer, as the pass would have,
+// unless the previous pass was skipped too. Passes q and q + 2 share a look-back buffer, so
+// after a skipped pass q - 1 the buffer of pass q + 1 is the one pass q - 1 found clean and
+// left untouched: the first pass's buffer is cleared by the histogram, the second's by the
+// first pass (run or skipped), and a pass that runs clears its successor's as it goes.
 template <int KB, int VB>
 __device__ __forceinline__ bool resolve_pass(const OnesweepParams& p, PassIO& io)
 {
@@ -99,7 +103,8 @@ __device__ __forceinline__ bool resolve_pass(const OnesweepParams& p, PassIO& io
   const uint32_t w = __ldcg(p.plan);
   if (w & PLAN_SKIP)
   {
-    if (p.lookback_next != nullptr)
+    const bool prev_skipped = p.plan_prev != nullptr && (__ldcg(p.plan_prev) & PLAN_SKIP) != 0u;
+    if (p.lookback_next != nullptr && !prev_skipped)
     {
       uint32_t* rows                    = p.lookback_next + (size_t) p.tile_row_base * RADIX_DIGITS;
       const unsigned long long words    = (unsigned long long) p.portion_tiles * RADIX_DIGITS;

@@ -331,6 +331,7 @@ void radix_sort_dispatch(const RadixPolicy& pol, const RadixKernels& ks, const R
       op.decode_out    = p == passes - 1;
       op.gate          = c.gate;
       op.plan          = &ctrl->plan[p];
+      op.plan_prev     = p > 0 ? &ctrl->plan[p - 1] : nullptr;
       for (int b = 0; b < 3; ++b)
       {
         op.key_bufs[b]   = key_bufs[b];

@@ -148,12 +148,14 @@ struct OnesweepParams
   int decode_out;             // last pass: keys are decoded on store
   KernelGate gate;
   // Pass plan (null: the pass runs with the buffers above). With a plan the pass reads its
-  // PLAN_* word: a skipped pass only clears its rows of lookback_next; a pass that runs
-  // takes keys_in / keys_out / values_in / values_out from these tables by the word's
-  // indices, and encode_in / decode_out from its flags.
+  // PLAN_* word: a skipped pass only clears its rows of lookback_next, and only when the
+  // previous pass ran (plan_prev: that pass's word, null for the first pass, which always
+  // clears); a pass that runs takes keys_in / keys_out / values_in / values_out from these
+  // tables by the word's indices, and encode_in / decode_out from its flags.
   const uint32_t* plan;
   const void* key_bufs[3];    // whole arrays
   const void* value_bufs[3];
+  const uint32_t* plan_prev;
 };
 
 struct SingleTileParams

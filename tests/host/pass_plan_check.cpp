@@ -128,6 +128,36 @@ void check(int P, int mode, uint32_t mask)
       fail(P, mode, mask, "a skippable pass runs without need, or none runs when needed");
     }
   }
+  // look-back buffers (passes q and q + 2 share one): every pass that runs must find its
+  // rows clean. Restated from resolve_pass (onesweep.cuh): the histogram clears the first
+  // pass's buffer, a pass that runs uses its own and clears its successor's, a skipped pass
+  // clears its successor's only when the previous pass ran (or it is the first pass).
+  bool dirty[2] = {true, true}; // left by an earlier sort in the same temporary storage
+  dirty[0]      = false;
+  for (int q = 0; q < P; ++q)
+  {
+    const bool has_next = q + 1 < P;
+    if (!(plan[q] & PLAN_SKIP))
+    {
+      if (dirty[q & 1])
+      {
+        fail(P, mode, mask, "a pass that runs finds its look-back rows dirty");
+      }
+      dirty[q & 1] = true;
+      if (has_next)
+      {
+        dirty[(q + 1) & 1] = false;
+      }
+    }
+    else
+    {
+      const bool prev_skipped = q > 0 && (plan[q - 1] & PLAN_SKIP);
+      if (has_next && !prev_skipped)
+      {
+        dirty[(q + 1) & 1] = false;
+      }
+    }
+  }
   if (extra == 1 && first >= 0)
   {
     // the extra pass is the first skippable one

@@ -2,7 +2,9 @@
 code the histogram kernel runs) compiled with g++ and checked for every pass count, buffer
 mode and set of skippable passes (tests/host/pass_plan_check.cpp): the result lands where
 running every pass puts it, the passes that run hand their buffers on in turn, the first
-encodes and the last decodes, and a skippable pass runs only when the buffer parity needs it."""
+encodes and the last decodes, a skippable pass runs only when the buffer parity needs it,
+and every pass that runs finds its look-back rows cleared although a skipped pass clears
+its successor's rows only after a pass that ran."""
 
 import shutil
 import subprocess
